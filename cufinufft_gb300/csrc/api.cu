@@ -1,0 +1,743 @@
+// api.cu -- the C ABI (include/cufinufft.h): plan, setpts, execute, destroy.
+//
+// Stage structure follows the reference (src/cufinufft.cu:78-637 and the
+// per-dimension drivers src/{1d,2d,3d}/cufinufft*d.cu): makeplan sizes the
+// fine grid, builds the cuFFT plan and the kernel's Fourier-series factors;
+// setpts bin-sorts the points; execute loops over batches of maxbatchsize
+// transforms doing spread -> FFT -> deconvolve (type 1) or amplify -> FFT ->
+// interp (type 2).  All device work is queued on one stream per plan; no
+// call inside execute synchronises the host.
+#include <cufft.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/cufinufft.h"
+#include "kernels.h"
+#include "planner.h"
+
+namespace cfg {
+
+template <typename T> struct Plan {
+  using C = cplx_t<T>;
+  int type = 0, dim = 0;
+  int N[3] = {1, 1, 1};
+  int nf[3] = {1, 1, 1};
+  int ntransf = 1, maxbatch = 1, iflag = 1;
+  cufinufft_opts opts;
+  SpreaderParams sp{};
+  int method = 0;  // method run: 1 (NU-point driven) or 2 (subproblem); 0 = invalid
+  int sort = 1;
+  int bs[3] = {1, 1, 1}, nb[3] = {1, 1, 1};
+  int nbins = 1;
+  int device = 0;
+  int M = 0, nsub = 0;
+  bool planned = false, pts_set = false;
+  cudaStream_t own = nullptr, stream = nullptr;
+  cufftHandle fft = 0, fft_rem = 0;
+  bool have_fft = false, have_fft_rem = false;
+  int rem = 0;
+  C* fw = nullptr;
+  T* fac[3] = {nullptr, nullptr, nullptr};
+  T* horner = nullptr;
+  // sorted points and bin tables
+  int* idx = nullptr;
+  int* i0[3] = {nullptr, nullptr, nullptr};
+  T* d[3] = {nullptr, nullptr, nullptr};
+  int* rank = nullptr;
+  size_t capM = 0;
+  int* count = nullptr;
+  int* start = nullptr;
+  int* sub_start = nullptr;
+  int* scan_tmp = nullptr;
+  int* sub_to_bin = nullptr;
+  size_t cap_sub = 0;
+  int* h_total = nullptr;  // pinned readback of the subproblem count
+  // stage timing (extension): events recorded around each stage of execute
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;   // free events
+  std::vector<cudaEvent_t> ev_live;   // groups of 4 per batch, not yet read
+  double stage_ms[3] = {0, 0, 0};     // spread|interp, fft, deconv|amplify
+  long long stage_batches = 0;
+};
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    ok = cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+#define CFG_CUDA(call)                                             \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) {                                       \
+      fprintf(stderr, "cufinufft: %s failed: %s\n", #call, cudaGetErrorString(e_)); \
+      return e_ == cudaErrorMemoryAllocation ? CUFINUFFT_ERR_ALLOC : CUFINUFFT_ERR_CUDA; \
+    }                                                              \
+  } while (0)
+
+#define CFG_CUFFT(call)                                            \
+  do {                                                             \
+    cufftResult r_ = (call);                                       \
+    if (r_ != CUFFT_SUCCESS) {                                     \
+      fprintf(stderr, "cufinufft: %s failed: cufftResult %d\n", #call, (int)r_); \
+      return r_ == CUFFT_ALLOC_FAILED ? CUFINUFFT_ERR_ALLOC : CUFINUFFT_ERR_CUFFT; \
+    }                                                              \
+  } while (0)
+
+template <typename T> constexpr bool is_single() { return sizeof(T) == 4; }
+
+template <typename T> cufftType fft_type();
+template <> cufftType fft_type<float>() { return CUFFT_C2C; }
+template <> cufftType fft_type<double>() { return CUFFT_Z2Z; }
+
+static cufftResult fft_exec(cufftHandle h, float2* data, int dir) {
+  return cufftExecC2C(h, (cufftComplex*)data, (cufftComplex*)data, dir);
+}
+static cufftResult fft_exec(cufftHandle h, double2* data, int dir) {
+  return cufftExecZ2Z(h, (cufftDoubleComplex*)data, (cufftDoubleComplex*)data, dir);
+}
+
+// Defaults, restating CUFINUFFT_DEFAULT_OPTS (src/cufinufft.cu:639-730).
+int default_opts(int type, int dim, cufinufft_opts* opts) {
+  if (opts == nullptr) return CUFINUFFT_ERR_ARG;
+  opts->upsampfac = 2.0;
+  opts->gpu_nstreams = 0;
+  opts->gpu_sort = 1;
+  opts->gpu_maxsubprobsize = 1024;
+  opts->gpu_obinsizex = -1;
+  opts->gpu_obinsizey = -1;
+  opts->gpu_obinsizez = -1;
+  opts->gpu_binsizex = -1;
+  opts->gpu_binsizey = -1;
+  opts->gpu_binsizez = -1;
+  opts->gpu_spreadinterponly = 0;
+  opts->gpu_kerevalmeth = 0;
+  opts->gpu_device_id = 0;
+  if (dim < 1 || dim > 3) return CUFINUFFT_ERR_ARG;
+  if (type == 1) opts->gpu_method = 2;
+  else if (type == 2) opts->gpu_method = 1;
+  else return CUFINUFFT_ERR_GENERIC;  // type 3 is not implemented (reference returns 1)
+  return 0;
+}
+
+// Bin sizes, restating SETUP_BINSIZE (src/cufinufft.cu:17-73): a value < 0
+// means "choose"; 1D 1024, 2D 32x32, 3D 16x16x2, 3D method 4 obin 8^3.
+static void setup_binsize(int dim, cufinufft_opts* o) {
+  if (dim == 1) {
+    if (o->gpu_binsizex < 0) o->gpu_binsizex = 1024;
+    o->gpu_binsizey = 1;
+    o->gpu_binsizez = 1;
+  } else if (dim == 2) {
+    if (o->gpu_binsizex < 0) o->gpu_binsizex = 32;
+    if (o->gpu_binsizey < 0) o->gpu_binsizey = 32;
+    o->gpu_binsizez = 1;
+  } else {
+    if (o->gpu_method == 4) {
+      if (o->gpu_obinsizex < 0) o->gpu_obinsizex = 8;
+      if (o->gpu_obinsizey < 0) o->gpu_obinsizey = 8;
+      if (o->gpu_obinsizez < 0) o->gpu_obinsizez = 8;
+      if (o->gpu_binsizex < 0) o->gpu_binsizex = 4;
+      if (o->gpu_binsizey < 0) o->gpu_binsizey = 4;
+      if (o->gpu_binsizez < 0) o->gpu_binsizez = 4;
+    } else {
+      if (o->gpu_binsizex < 0) o->gpu_binsizex = 16;
+      if (o->gpu_binsizey < 0) o->gpu_binsizey = 16;
+      if (o->gpu_binsizez < 0) o->gpu_binsizez = 2;
+    }
+  }
+}
+
+template <typename T> static void free_points(Plan<T>* p) {
+  cudaFree(p->idx);
+  cudaFree(p->rank);
+  p->idx = p->rank = nullptr;
+  for (int k = 0; k < 3; ++k) {
+    cudaFree(p->i0[k]);
+    cudaFree(p->d[k]);
+    p->i0[k] = nullptr;
+    p->d[k] = nullptr;
+  }
+  p->capM = 0;
+}
+
+template <typename T> static void release(Plan<T>* p) {
+  if (p->have_fft) cufftDestroy(p->fft);
+  if (p->have_fft_rem) cufftDestroy(p->fft_rem);
+  p->have_fft = p->have_fft_rem = false;
+  cudaFree(p->fw);
+  p->fw = nullptr;
+  for (int k = 0; k < 3; ++k) {
+    cudaFree(p->fac[k]);
+    p->fac[k] = nullptr;
+  }
+  cudaFree(p->horner);
+  p->horner = nullptr;
+  free_points(p);
+  cudaFree(p->count);
+  cudaFree(p->start);
+  cudaFree(p->sub_start);
+  cudaFree(p->scan_tmp);
+  cudaFree(p->sub_to_bin);
+  p->count = p->start = p->sub_start = p->scan_tmp = p->sub_to_bin = nullptr;
+  p->cap_sub = 0;
+  if (p->h_total) cudaFreeHost(p->h_total);
+  p->h_total = nullptr;
+  for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->ev_live) cudaEventDestroy(e);
+  p->ev_pool.clear();
+  p->ev_live.clear();
+  if (p->own) cudaStreamDestroy(p->own);
+  p->own = p->stream = nullptr;
+  p->planned = p->pts_set = false;
+}
+
+template <typename T> static long long grid_cells(const Plan<T>* p) {
+  return (long long)p->nf[0] * p->nf[1] * p->nf[2];
+}
+
+template <typename T>
+static int make_fft(Plan<T>* p, int batch, cufftHandle* h) {
+  int n[3], dist = (int)grid_cells(p);
+  for (int k = 0; k < p->dim; ++k) n[k] = p->nf[p->dim - 1 - k];  // slowest first
+  CFG_CUFFT(cufftPlanMany(h, p->dim, n, n, 1, dist, n, 1, dist, fft_type<T>(), batch));
+  CFG_CUFFT(cufftSetStream(*h, p->stream));
+  return 0;
+}
+
+template <typename T>
+static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int iflag, int ntransf,
+                         double tol, int maxbatchsize, const cufinufft_opts* opts) {
+  p->type = type;
+  p->dim = dim;
+  if (opts) p->opts = *opts;
+  else default_opts(type, dim, &p->opts);
+  int ier = setup_spreader(tol, p->opts.upsampfac, p->opts.gpu_kerevalmeth, is_single<T>(), &p->sp);
+  if (ier > 1) return ier;
+  for (int k = 0; k < dim; ++k) p->N[k] = nmodes[k];
+  setup_binsize(dim, &p->opts);
+
+  // method actually run (src/2d/spread2d_wrapper.cu:99-164,
+  // src/3d/spread3d_wrapper.cu:101-160, src/*/interp*_wrapper.cu):
+  const int m = p->opts.gpu_method;
+  p->sort = p->opts.gpu_sort;
+  int bins_from_obin = 0;
+  if (type == 1) {
+    if (m == 1 || m == 2) p->method = m;
+    else if (m == 3 && dim == 2) p->method = 2;
+    else if (m == 4 && dim == 3) { p->method = 2; bins_from_obin = 1; }
+    else p->method = 0;
+  } else {
+    if (m == 1) p->method = 1;
+    else if (m == 2 && dim > 1) p->method = 2;
+    else p->method = 0;
+  }
+  if (p->method == 2) p->sort = 1;
+
+  const int obin[3] = {p->opts.gpu_obinsizex, p->opts.gpu_obinsizey, p->opts.gpu_obinsizez};
+  for (int k = 0; k < dim; ++k) {
+    if (bins_from_obin && obin[k] <= 0) return CUFINUFFT_ERR_ARG;
+    p->nf[k] = set_nf_type12(p->N[k], p->opts.upsampfac, p->sp.ns, m, bins_from_obin ? obin[k] : 1);
+  }
+  const int bsz[3] = {p->opts.gpu_binsizex, p->opts.gpu_binsizey, p->opts.gpu_binsizez};
+  for (int k = 0; k < 3; ++k) {
+    if (k < dim) {
+      int b = bins_from_obin ? obin[k] : bsz[k];
+      if (b <= 0) return CUFINUFFT_ERR_GENERIC;  // reference: "invalid binsize"
+      if (b > p->nf[k]) b = p->nf[k];
+      p->bs[k] = b;
+      p->nb[k] = (p->nf[k] + b - 1) / b;
+    } else {
+      p->bs[k] = 1;
+      p->nb[k] = 1;
+    }
+  }
+  long long nbins = (long long)p->nb[0] * p->nb[1] * p->nb[2];
+  if (nbins > (1LL << 24)) return CUFINUFFT_ERR_ARG;
+  p->nbins = (int)nbins;
+  if (p->method == 2 && p->opts.gpu_maxsubprobsize <= 0) return CUFINUFFT_ERR_ARG;
+
+  p->iflag = iflag >= 0 ? 1 : -1;
+  p->ntransf = ntransf;
+  if (maxbatchsize == 0) maxbatchsize = std::min(ntransf, 8);
+  p->maxbatch = std::min(maxbatchsize, ntransf);
+  p->rem = ntransf % p->maxbatch;
+
+  CFG_CUDA(cudaStreamCreate(&p->own));  // blocking: ordered after the legacy default stream
+  p->stream = p->own;
+  CFG_CUDA(cudaMallocHost(&p->h_total, sizeof(int)));
+
+  const long long Nf = grid_cells(p);
+  CFG_CUDA(cudaMalloc(&p->fw, sizeof(cplx_t<T>) * (size_t)Nf * p->maxbatch));
+  for (int k = 0; k < dim; ++k) CFG_CUDA(cudaMalloc(&p->fac[k], sizeof(T) * (size_t)p->N[k]));
+  CFG_CUDA(cudaMalloc(&p->count, sizeof(int) * (size_t)p->nbins));
+  CFG_CUDA(cudaMalloc(&p->start, sizeof(int) * ((size_t)p->nbins + 1)));
+  CFG_CUDA(cudaMalloc(&p->sub_start, sizeof(int) * ((size_t)p->nbins + 1)));
+  CFG_CUDA(cudaMalloc(&p->scan_tmp, sizeof(int) * (size_t)scan_tmp_ints(p->nbins)));
+
+  int e = make_fft(p, p->maxbatch, &p->fft);
+  if (e) return e;
+  p->have_fft = true;
+  if (p->rem) {
+    e = make_fft(p, p->rem, &p->fft_rem);
+    if (e) return e;
+    p->have_fft_rem = true;
+  }
+
+  FseriesNodes nodes;
+  fseries_nodes(p->sp, &nodes);
+  CFG_CUDA(launch_fseries<T>(nodes, dim, p->nf, p->N, p->fac[0], p->fac[1], p->fac[2], p->stream));
+
+  std::vector<T> hh;
+  if (p->opts.gpu_kerevalmeth == 1) {
+    const int deg = horner_degree<T>(p->sp.ns);
+    std::vector<double> cd = horner_fit(p->sp, deg);
+    hh.assign(cd.begin(), cd.end());
+    CFG_CUDA(cudaMalloc(&p->horner, sizeof(T) * hh.size()));
+    CFG_CUDA(cudaMemcpyAsync(p->horner, hh.data(), sizeof(T) * hh.size(), cudaMemcpyHostToDevice,
+                             p->stream));
+  }
+  CFG_CUDA(cudaStreamSynchronize(p->stream));
+  p->planned = true;
+  return 0;
+}
+
+template <typename T>
+static int ensure_points(Plan<T>* p, int M) {
+  if ((size_t)M <= p->capM && p->idx) return 0;
+  free_points(p);
+  size_t n = (size_t)std::max(M, 1);
+  CFG_CUDA(cudaMalloc(&p->idx, sizeof(int) * n));
+  CFG_CUDA(cudaMalloc(&p->rank, sizeof(int) * n));
+  for (int k = 0; k < p->dim; ++k) {
+    CFG_CUDA(cudaMalloc(&p->i0[k], sizeof(int) * n));
+    CFG_CUDA(cudaMalloc(&p->d[k], sizeof(T) * n));
+  }
+  p->capM = n;
+  return 0;
+}
+
+template <typename T>
+static AxisMap<T> axis_map(int nf, int ns) {
+  AxisMap<T> a;
+  const double S = (double)nf / (2.0 * M_PI);
+  a.s_hi = (T)S;
+  a.s_lo = (T)(S - (double)a.s_hi);
+  a.o_lo = (T)(1.5 * nf);
+  a.o_mid = (T)(0.5 * nf);
+  a.o_hi = (T)(-0.5 * nf);
+  a.half_int = ns / 2;
+  a.half_frac = (ns % 2) ? T(0.5) : T(0);
+  a.nf = nf;
+  return a;
+}
+
+template <typename T>
+static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
+  if (!p->planned) return CUFINUFFT_ERR_GENERIC;
+  if (M < 0) return CUFINUFFT_ERR_ARG;
+  const T* xs[3] = {x, y, z};
+  for (int k = 0; k < p->dim; ++k)
+    if (M > 0 && xs[k] == nullptr) return CUFINUFFT_ERR_ARG;
+  p->pts_set = false;
+  int e = ensure_points(p, M);
+  if (e) return e;
+  p->M = M;
+  p->nsub = 0;
+  PlaceArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  for (int k = 0; k < 3; ++k) {
+    a.x[k] = k < p->dim ? xs[k] : nullptr;
+    a.ax[k] = axis_map<T>(p->nf[k], p->sp.ns);
+    a.bs[k] = p->bs[k];
+    a.nb[k] = p->nb[k];
+    a.i0[k] = p->i0[k];
+    a.d[k] = p->d[k];
+  }
+  a.dim = p->dim;
+  a.M = M;
+  a.idx = p->idx;
+  a.count = p->count;
+  a.rank = p->rank;
+  a.start = p->start;
+  if (p->method == 1 && p->sort == 0) {
+    CFG_CUDA(launch_place_unsorted<T>(a, p->stream));
+  } else {
+    CFG_CUDA(cudaMemsetAsync(p->count, 0, sizeof(int) * (size_t)p->nbins, p->stream));
+    CFG_CUDA(launch_bin_count<T>(a, p->stream));
+    CFG_CUDA(launch_scan(p->count, p->start, p->nbins, 0, 1, p->scan_tmp, p->stream));
+    CFG_CUDA(launch_permute<T>(a, p->stream));
+    if (p->method == 2) {
+      const int ms = p->opts.gpu_maxsubprobsize;
+      CFG_CUDA(launch_scan(p->count, p->sub_start, p->nbins, 1, ms, p->scan_tmp, p->stream));
+      CFG_CUDA(cudaMemcpyAsync(p->h_total, p->sub_start + p->nbins, sizeof(int),
+                               cudaMemcpyDeviceToHost, p->stream));
+      CFG_CUDA(cudaStreamSynchronize(p->stream));
+      const int nsub = *p->h_total;
+      if ((size_t)nsub > p->cap_sub) {
+        cudaFree(p->sub_to_bin);
+        p->sub_to_bin = nullptr;
+        p->cap_sub = 0;
+        CFG_CUDA(cudaMalloc(&p->sub_to_bin, sizeof(int) * (size_t)nsub));
+        p->cap_sub = nsub;
+      }
+      CFG_CUDA(launch_sub_to_bin(p->sub_start, p->nbins, nsub, p->sub_to_bin, p->stream));
+      p->nsub = nsub;
+    }
+  }
+  CFG_CUDA(cudaGetLastError());
+  p->pts_set = true;
+  return 0;
+}
+
+template <typename T>
+static SpreadArgs<T> spread_args(Plan<T>* p) {
+  SpreadArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.pts.idx = p->idx;
+  for (int k = 0; k < 3; ++k) {
+    a.pts.i0[k] = p->i0[k];
+    a.pts.d[k] = p->d[k];
+    a.bins.bs[k] = p->bs[k];
+    a.bins.nb[k] = p->nb[k];
+    a.g.nf[k] = p->nf[k];
+  }
+  a.pts.M = p->M;
+  a.bins.nbins = p->nbins;
+  a.bins.count = p->count;
+  a.bins.start = p->start;
+  a.bins.sub_start = p->sub_start;
+  a.bins.sub_to_bin = p->sub_to_bin;
+  a.bins.nsub = p->nsub;
+  a.bins.maxsub = p->opts.gpu_maxsubprobsize;
+  a.kc.beta = (T)p->sp.beta;
+  a.kc.c = (T)p->sp.c;
+  a.kc.horner = p->horner;
+  a.g.Nf = grid_cells(p);
+  a.M = p->M;
+  return a;
+}
+
+template <typename T>
+static cudaError_t run_spread(Plan<T>* p, const SpreadArgs<T>& a) {
+  switch (p->dim) {
+    case 1: return spread_dim<T, 1>(p->method, p->sp.ns, a, p->stream);
+    case 2: return spread_dim<T, 2>(p->method, p->sp.ns, a, p->stream);
+    default: return spread_dim<T, 3>(p->method, p->sp.ns, a, p->stream);
+  }
+}
+
+template <typename T>
+static cudaError_t run_interp(Plan<T>* p, const SpreadArgs<T>& a) {
+  switch (p->dim) {
+    case 1: return interp_dim<T, 1>(p->method, p->sp.ns, a, p->stream);
+    case 2: return interp_dim<T, 2>(p->method, p->sp.ns, a, p->stream);
+    default: return interp_dim<T, 3>(p->method, p->sp.ns, a, p->stream);
+  }
+}
+
+static int max_smem_optin(int device) {
+  int v = 0;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) return 48 * 1024;
+  return v;
+}
+
+template <typename T>
+static cudaEvent_t take_event(Plan<T>* p) {
+  cudaEvent_t e = nullptr;
+  if (!p->ev_pool.empty()) {
+    e = p->ev_pool.back();
+    p->ev_pool.pop_back();
+  } else if (cudaEventCreate(&e) != cudaSuccess) {
+    return nullptr;
+  }
+  p->ev_live.push_back(e);
+  return e;
+}
+
+template <typename T>
+static void mark(Plan<T>* p, cudaEvent_t e) {
+  if (e) cudaEventRecord(e, p->stream);
+}
+
+// Waits for the recorded batches and folds their stage times into stage_ms.
+template <typename T>
+static int collect_times(Plan<T>* p) {
+  const size_t n = p->ev_live.size() / 4 * 4;
+  for (size_t i = 0; i < n; i += 4) {
+    cudaEvent_t* e = &p->ev_live[i];
+    CFG_CUDA(cudaEventSynchronize(e[3]));
+    float a = 0, b = 0, c = 0;
+    CFG_CUDA(cudaEventElapsedTime(&a, e[0], e[1]));
+    CFG_CUDA(cudaEventElapsedTime(&b, e[1], e[2]));
+    CFG_CUDA(cudaEventElapsedTime(&c, e[2], e[3]));
+    // event order: type 1 = [memset+spread | fft | deconv], type 2 =
+    // [amplify | fft | interp]
+    if (p->type == 1) {
+      p->stage_ms[0] += a;
+      p->stage_ms[2] += c;
+    } else {
+      p->stage_ms[2] += a;
+      p->stage_ms[0] += c;
+    }
+    p->stage_ms[1] += b;
+    p->stage_batches += 1;
+  }
+  for (size_t i = 0; i < n; ++i) p->ev_pool.push_back(p->ev_live[i]);
+  p->ev_live.erase(p->ev_live.begin(), p->ev_live.begin() + n);
+  return 0;
+}
+
+template <typename T>
+static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
+  if (!p->planned) return CUFINUFFT_ERR_GENERIC;
+  if (p->type != 1 && p->type != 2) return CUFINUFFT_ERR_GENERIC;
+  if (p->method == 0) return CUFINUFFT_ERR_METHOD;
+  if (!p->pts_set) return CUFINUFFT_ERR_GENERIC;
+  if (p->M > 0 && c == nullptr) return CUFINUFFT_ERR_ARG;
+  if (fk == nullptr) return CUFINUFFT_ERR_ARG;
+  if (p->method == 2) {
+    size_t bytes = tile_cells(p->dim, p->sp.ns, p->bs) * sizeof(cplx_t<T>);
+    if (bytes > (size_t)max_smem_optin(p->device)) return CUFINUFFT_ERR_SHMEM;
+  }
+  const long long Nf = grid_cells(p);
+  const long long Nm = (long long)p->N[0] * p->N[1] * p->N[2];
+  SpreadArgs<T> a = spread_args(p);
+  for (int b0 = 0; b0 < p->ntransf; b0 += p->maxbatch) {
+    const int B = std::min(p->maxbatch, p->ntransf - b0);
+    cufftHandle h = (B == p->maxbatch) ? p->fft : p->fft_rem;
+    a.ntr = B;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    if (p->timing)
+      for (int k = 0; k < 4; ++k) ev[k] = take_event(p);
+    mark(p, ev[0]);
+    if (p->type == 1) {
+      a.c_in = c + (size_t)b0 * p->M;
+      a.fw = p->fw;
+      CFG_CUDA(cudaMemsetAsync(p->fw, 0, sizeof(cplx_t<T>) * (size_t)Nf * B, p->stream));
+      CFG_CUDA(run_spread(p, a));
+      mark(p, ev[1]);
+      CFG_CUFFT(fft_exec(h, p->fw, p->iflag));
+      mark(p, ev[2]);
+      CFG_CUDA(launch_deconvolve<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
+                                    p->fac[1], p->fac[2], B, p->stream));
+    } else {
+      CFG_CUDA(launch_amplify<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
+                                 p->fac[1], p->fac[2], B, p->stream));
+      mark(p, ev[1]);
+      CFG_CUFFT(fft_exec(h, p->fw, p->iflag));
+      mark(p, ev[2]);
+      a.fw_in = p->fw;
+      a.c_out = c + (size_t)b0 * p->M;
+      CFG_CUDA(run_interp(p, a));
+    }
+    mark(p, ev[3]);
+  }
+  return 0;
+}
+
+template <typename T>
+static void fill_info(const Plan<T>* p, cufinufft_plan_info* info) {
+  std::memset(info, 0, sizeof(*info));
+  info->type = p->type;
+  info->dim = p->dim;
+  info->ms = p->N[0];
+  info->mt = p->N[1];
+  info->mu = p->N[2];
+  info->nf1 = p->nf[0];
+  info->nf2 = p->nf[1];
+  info->nf3 = p->nf[2];
+  info->ns = p->sp.ns;
+  info->M = p->M;
+  info->ntransf = p->ntransf;
+  info->maxbatchsize = p->maxbatch;
+  info->method = p->method;
+  info->sort = p->sort;
+  info->binsizex = p->bs[0];
+  info->binsizey = p->bs[1];
+  info->binsizez = p->bs[2];
+  info->nbins = p->nbins;
+  info->nsubprob = p->nsub;
+  info->kerevalmeth = p->opts.gpu_kerevalmeth;
+  info->beta = p->sp.beta;
+  info->es_c = p->sp.c;
+}
+
+template <typename T, typename H>
+static int makeplan_entry(int type, int dim, int* nmodes, int iflag, int ntransf, double tol,
+                          int maxbatchsize, H** plan, cufinufft_opts* opts) {
+  if (plan == nullptr) return CUFINUFFT_ERR_ARG;
+  *plan = nullptr;
+  if (dim < 1 || dim > 3 || nmodes == nullptr || ntransf < 1 || maxbatchsize < 0)
+    return CUFINUFFT_ERR_ARG;
+  for (int k = 0; k < dim; ++k)
+    if (nmodes[k] < 1) return CUFINUFFT_ERR_ARG;
+  H* h = new (std::nothrow) H();
+  if (!h) return CUFINUFFT_ERR_ALLOC;
+  *plan = h;
+  Plan<T>* p = &h->p;
+  p->device = opts ? opts->gpu_device_id : 0;
+  if (type != 1 && type != 2) {
+    p->type = type;
+    p->dim = dim;
+    return CUFINUFFT_ERR_GENERIC;  // type 3 is not implemented (src/cufinufft.cu:533)
+  }
+  DeviceGuard g(p->device);
+  if (!g.ok) return CUFINUFFT_ERR_CUDA;
+  int ier = makeplan_impl<T>(p, type, dim, nmodes, iflag, ntransf, tol, maxbatchsize, opts);
+  if (ier) release(p);
+  return ier;
+}
+
+}  // namespace cfg
+
+struct cufinufft_plan_s {
+  cfg::Plan<double> p;
+};
+struct cufinufftf_plan_s {
+  cfg::Plan<float> p;
+};
+
+using cfg::DeviceGuard;
+
+template <typename H>
+static int setpts_entry(H* h, int M, decltype(h->p.d[0]) x, decltype(h->p.d[0]) y,
+                        decltype(h->p.d[0]) z) {
+  if (h == nullptr) return CUFINUFFT_ERR_GENERIC;
+  DeviceGuard g(h->p.device);
+  if (!g.ok) return CUFINUFFT_ERR_CUDA;
+  return cfg::setpts_impl(&h->p, M, x, y, z);
+}
+
+template <typename H, typename C>
+static int execute_entry(H* h, C* c, C* fk) {
+  if (h == nullptr) return CUFINUFFT_ERR_GENERIC;
+  DeviceGuard g(h->p.device);
+  if (!g.ok) return CUFINUFFT_ERR_CUDA;
+  return cfg::execute_impl(&h->p, c, fk);
+}
+
+template <typename H>
+static int destroy_entry(H* h) {
+  if (h == nullptr) return 1;  // reference: cannot destroy a NULL plan
+  {
+    DeviceGuard g(h->p.device);
+    cfg::release(&h->p);
+  }
+  delete h;
+  return 0;
+}
+
+template <typename H>
+static int stage_times_entry(H* h, double* ms, long long* batches, int reset) {
+  if (!h || !ms) return CUFINUFFT_ERR_GENERIC;
+  DeviceGuard g(h->p.device);
+  int e = cfg::collect_times(&h->p);
+  if (e) return e;
+  for (int k = 0; k < 3; ++k) ms[k] = h->p.stage_ms[k];
+  if (batches) *batches = h->p.stage_batches;
+  if (reset) {
+    for (int k = 0; k < 3; ++k) h->p.stage_ms[k] = 0;
+    h->p.stage_batches = 0;
+  }
+  return 0;
+}
+
+extern "C" {
+
+int cufinufft_default_opts(int type, int dim, cufinufft_opts* opts) {
+  return cfg::default_opts(type, dim, opts);
+}
+int cufinufftf_default_opts(int type, int dim, cufinufft_opts* opts) {
+  return cfg::default_opts(type, dim, opts);
+}
+
+int cufinufft_makeplan(int type, int dim, int* nmodes, int iflag, int ntransf, double tol,
+                       int maxbatchsize, cufinufft_plan* plan, cufinufft_opts* opts) {
+  return cfg::makeplan_entry<double>(type, dim, nmodes, iflag, ntransf, tol, maxbatchsize, plan,
+                                     opts);
+}
+int cufinufftf_makeplan(int type, int dim, int* nmodes, int iflag, int ntransf, float tol,
+                        int maxbatchsize, cufinufftf_plan* plan, cufinufft_opts* opts) {
+  return cfg::makeplan_entry<float>(type, dim, nmodes, iflag, ntransf, (double)tol, maxbatchsize,
+                                    plan, opts);
+}
+
+int cufinufft_setpts(int M, double* x, double* y, double* z, int N, double* s, double* t, double* u,
+                     cufinufft_plan plan) {
+  (void)N; (void)s; (void)t; (void)u;
+  return setpts_entry(plan, M, x, y, z);
+}
+int cufinufftf_setpts(int M, float* x, float* y, float* z, int N, float* s, float* t, float* u,
+                      cufinufftf_plan plan) {
+  (void)N; (void)s; (void)t; (void)u;
+  return setpts_entry(plan, M, x, y, z);
+}
+
+int cufinufft_execute(cuDoubleComplex* c, cuDoubleComplex* fk, cufinufft_plan plan) {
+  return execute_entry(plan, reinterpret_cast<double2*>(c), reinterpret_cast<double2*>(fk));
+}
+int cufinufftf_execute(cuFloatComplex* c, cuFloatComplex* fk, cufinufftf_plan plan) {
+  return execute_entry(plan, reinterpret_cast<float2*>(c), reinterpret_cast<float2*>(fk));
+}
+
+int cufinufft_destroy(cufinufft_plan plan) { return destroy_entry(plan); }
+int cufinufftf_destroy(cufinufftf_plan plan) { return destroy_entry(plan); }
+
+int cufinufft_set_stream(cufinufft_plan plan, cudaStream_t stream) {
+  if (!plan || !plan->p.planned) return CUFINUFFT_ERR_GENERIC;
+  plan->p.stream = stream ? stream : plan->p.own;
+  if (plan->p.have_fft && cufftSetStream(plan->p.fft, plan->p.stream) != CUFFT_SUCCESS) return CUFINUFFT_ERR_CUFFT;
+  if (plan->p.have_fft_rem && cufftSetStream(plan->p.fft_rem, plan->p.stream) != CUFFT_SUCCESS)
+    return CUFINUFFT_ERR_CUFFT;
+  return 0;
+}
+int cufinufftf_set_stream(cufinufftf_plan plan, cudaStream_t stream) {
+  if (!plan || !plan->p.planned) return CUFINUFFT_ERR_GENERIC;
+  plan->p.stream = stream ? stream : plan->p.own;
+  if (plan->p.have_fft && cufftSetStream(plan->p.fft, plan->p.stream) != CUFFT_SUCCESS) return CUFINUFFT_ERR_CUFFT;
+  if (plan->p.have_fft_rem && cufftSetStream(plan->p.fft_rem, plan->p.stream) != CUFFT_SUCCESS)
+    return CUFINUFFT_ERR_CUFFT;
+  return 0;
+}
+
+int cufinufft_set_timing(cufinufft_plan plan, int on) {
+  if (!plan) return CUFINUFFT_ERR_GENERIC;
+  plan->p.timing = on != 0;
+  return 0;
+}
+int cufinufftf_set_timing(cufinufftf_plan plan, int on) {
+  if (!plan) return CUFINUFFT_ERR_GENERIC;
+  plan->p.timing = on != 0;
+  return 0;
+}
+
+int cufinufft_stage_times(cufinufft_plan plan, double* ms, long long* batches, int reset) {
+  return stage_times_entry(plan, ms, batches, reset);
+}
+int cufinufftf_stage_times(cufinufftf_plan plan, double* ms, long long* batches, int reset) {
+  return stage_times_entry(plan, ms, batches, reset);
+}
+
+int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info) {
+  if (!plan || !info) return CUFINUFFT_ERR_GENERIC;
+  cfg::fill_info(&plan->p, info);
+  return 0;
+}
+int cufinufftf_get_info(cufinufftf_plan plan, cufinufft_plan_info* info) {
+  if (!plan || !info) return CUFINUFFT_ERR_GENERIC;
+  cfg::fill_info(&plan->p, info);
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,140 @@
+// device_common.cuh -- device-side building blocks shared by the setpts,
+// spread, interp and deconvolution kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nufft_types.h"
+
+namespace cfg {
+
+// ---- exact-rounding arithmetic (never contracted into FMAs) --------------
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float floor_t(float a) { return floorf(a); }
+__device__ __forceinline__ double floor_t(double a) { return floor(a); }
+__device__ __forceinline__ float ceil_t(float a) { return ceilf(a); }
+__device__ __forceinline__ double ceil_t(double a) { return ceil(a); }
+
+// pi rounded to the plan precision: the fold branch compares against it, as
+// the reference's RESCALE macro does with PI = (FLT)M_PI
+// (contrib/spreadinterp.h:36-38, contrib/utils.h:21).
+template <typename T> __device__ __forceinline__ T pi_t();
+template <> __device__ __forceinline__ float pi_t<float>() { return 3.14159265358979323846f; }
+template <> __device__ __forceinline__ double pi_t<double>() { return 3.14159265358979323846; }
+
+// Fine-grid placement of one coordinate.  The reference computes the
+// rescaled position t = (x/(2 pi) + shift) * nf (shift 0.5, or 1.5 / -0.5 to
+// fold [-3pi,-pi) and [pi,3pi)), first tap i0 = ceil(t - ns/2) and tap
+// offsets i0 + j - t (src/2d/spreadinterp2d.cu:22-33).  Here t is carried as
+// an unevaluated sum t_hi + t_lo (error-free product and sum), so the stored
+// offset d = i0 - t + ns/2 in [0,1) keeps ~1 ulp of [0,1) even in FP32,
+// where a rounded t in [0, nf) would lose log2(nf) bits.
+//   i0 is returned wrapped into [0, nf); tap j sits at (i0 + j) mod nf with
+//   kernel argument d - ns/2 + j.
+template <typename T>
+__device__ __forceinline__ void place_coord(T x, const AxisMap<T>& a, int& i0, T& d) {
+  const T pi = pi_t<T>();
+  T o = (x < -pi) ? a.o_lo : ((x >= pi) ? a.o_hi : a.o_mid);
+  T p_hi = mul_rn(x, a.s_hi);
+  T p_err = fma_rn(x, a.s_hi, -p_hi);
+  T p_lo = fma_rn(x, a.s_lo, p_err);
+  T t_hi = add_rn(p_hi, o);
+  T bb = sub_rn(t_hi, p_hi);
+  T err = add_rn(sub_rn(p_hi, sub_rn(t_hi, bb)), sub_rn(o, bb));
+  T t_lo = add_rn(err, p_lo);
+  T fl = floor_t(t_hi);
+  T g = add_rn(sub_rn(t_hi, fl), t_lo);   // fractional position ~[0,1)
+  T gg = sub_rn(g, a.half_frac);          // minus the fractional part of ns/2
+  T cg = ceil_t(gg);
+  d = sub_rn(cg, gg);                     // in [0, 1)
+  int i = (int)fl + (int)cg - a.half_int;
+  if (i < 0) i += a.nf;
+  if (i >= a.nf) i -= a.nf;
+  // points outside [-3pi,3pi) (or non-finite ones) still land in [0, nf):
+  // every grid access stays in bounds whatever the input
+  if (i < 0 || i >= a.nf) i = ((i % a.nf) + a.nf) % a.nf;
+  i0 = i;
+}
+
+// ---- ES kernel values -----------------------------------------------------
+__device__ __forceinline__ float es_exp(float z, float beta) { return expf(beta * sqrtf(1.0f - z)); }
+__device__ __forceinline__ double es_exp(double z, double beta) { return exp(beta * sqrt(1.0 - z)); }
+
+// ker[j] = phi(d - ns/2 + j), j = 0..NS-1, phi(x) = exp(beta*sqrt(1-c x^2))
+// for |x| < ns/2 and 0 outside (src/cuspreadinterp.h:6-40).  With
+// horner != nullptr the values come from the plan's fitted piecewise
+// polynomials in z = 2d - 1 (coefficient k of tap j at horner[k*NS + j],
+// highest degree first, HDEG+1 rows).
+template <typename T, int NS, int HDEG>
+__device__ __forceinline__ void kernel_row(T d, const KernelCoeffs<T>& kc, T* ker) {
+  if (kc.horner != nullptr) {
+    const T z = T(2) * d - T(1);
+#pragma unroll
+    for (int j = 0; j < NS; ++j) ker[j] = __ldg(kc.horner + j);
+#pragma unroll
+    for (int k = 1; k <= HDEG; ++k) {
+#pragma unroll
+      for (int j = 0; j < NS; ++j) ker[j] = fma_rn(ker[j], z, __ldg(kc.horner + k * NS + j));
+    }
+  } else {
+    const T x0 = d - T(0.5) * T(NS);
+#pragma unroll
+    for (int j = 0; j < NS; ++j) {
+      T x = x0 + T(j);
+      T z = kc.c * x * x;
+      ker[j] = (z < T(1)) ? es_exp(z, kc.beta) : T(0);
+    }
+  }
+}
+
+// One kernel value phi(d - ns/2 + j) for a runtime tap index j (used along
+// the outermost axis of 3D loops, which are not unrolled).
+template <typename T, int NS, int HDEG>
+__device__ __forceinline__ T kernel_tap(T d, int j, const KernelCoeffs<T>& kc) {
+  if (kc.horner != nullptr) {
+    const T z = T(2) * d - T(1);
+    T v = __ldg(kc.horner + j);
+#pragma unroll
+    for (int k = 1; k <= HDEG; ++k) v = fma_rn(v, z, __ldg(kc.horner + k * NS + j));
+    return v;
+  }
+  const T x = d - T(0.5) * T(NS) + T(j);
+  const T z = kc.c * x * x;
+  return (z < T(1)) ? es_exp(z, kc.beta) : T(0);
+}
+
+// ---- atomics ---------------------------------------------------------------
+// Complex add into global memory: one vector reduction for FP32 (sm_90+),
+// two scalar reductions for FP64.
+__device__ __forceinline__ void red_add(float2* p, float re, float im) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(re), "f"(im) : "memory");
+}
+__device__ __forceinline__ void red_add(double2* p, double re, double im) {
+  atomicAdd(&p->x, re);
+  atomicAdd(&p->y, im);
+}
+
+// Shared-memory complex add.
+__device__ __forceinline__ void smem_add(float2* p, float re, float im) {
+  atomicAdd(&p->x, re);
+  atomicAdd(&p->y, im);
+}
+__device__ __forceinline__ void smem_add(double2* p, double re, double im) {
+  atomicAdd(&p->x, re);
+  atomicAdd(&p->y, im);
+}
+
+__device__ __forceinline__ int wrap_idx(int i, int n) {
+  if (i >= n) i -= n;
+  return i;
+}
+
+}  // namespace cfg

@@ -1,0 +1,90 @@
+// nufft_types.h -- plain-data types shared by host code and kernels.
+#pragma once
+
+#include <cuComplex.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cfg {
+
+constexpr int kMaxNS = 16;      // widest kernel (reference MAX_NSPREAD)
+constexpr int kMaxNQuad = 100;  // Gauss-Legendre nodes cap (MAX_NQUAD)
+
+template <typename T> struct cplx;
+template <> struct cplx<float> { using type = float2; };
+template <> struct cplx<double> { using type = double2; };
+template <typename T> using cplx_t = typename cplx<T>::type;
+
+// Degree of the fitted piecewise polynomials (kerevalmeth 1).  The fit error
+// reaches the kernel's own truncation level exp(-beta) ~ 10^-ns by degree
+// ns+1 (FP32) and ns+2 (FP64); one more degree is kept as margin.
+template <typename T> constexpr int horner_degree(int ns) {
+  return sizeof(T) == 4 ? ns + 2 : ns + 3;
+}
+
+// Constants that place one coordinate axis on the fine grid (see
+// place_coord in device_common.cuh).  s_hi + s_lo = nf/(2 pi); o_* = nf *
+// {1.5, 0.5, -0.5} for x < -pi, -pi <= x < pi, x >= pi; ns/2 = half_int +
+// half_frac.
+template <typename T> struct AxisMap {
+  T s_hi, s_lo, o_lo, o_mid, o_hi, half_frac;
+  int nf, half_int;
+};
+
+// Kernel-evaluation constants: phi(x) = exp(beta*sqrt(1 - c x^2)), or the
+// fitted polynomials when horner != nullptr.
+template <typename T> struct KernelCoeffs {
+  T beta, c;
+  const T* horner;
+};
+
+// Bin-sorted points in plan memory (written by setpts).
+template <typename T> struct SortedPts {
+  const int* idx;     // sorted position -> caller's point index
+  const int* i0[3];   // first tap per axis, wrapped into [0, nf)
+  const T* d[3];      // tap offset per axis in [0,1)
+  int M;
+};
+
+// Fine-grid geometry and bin/subproblem tables.
+struct GridGeom {
+  int nf[3];
+  long long Nf;       // nf1*nf2*nf3
+};
+
+struct BinTables {
+  int bs[3];          // bin size (cells) per axis
+  int nb[3];          // bins per axis
+  int nbins;
+  const int* count;       // points per bin            [nbins]
+  const int* start;       // exclusive scan of count   [nbins+1]
+  const int* sub_start;   // exclusive scan of subproblems per bin [nbins+1]
+  const int* sub_to_bin;  // subproblem -> bin          [nsub]
+  int nsub;
+  int maxsub;             // points per subproblem cap
+};
+
+// Everything a spread or interp launch needs.
+template <typename T> struct SpreadArgs {
+  SortedPts<T> pts;
+  BinTables bins;
+  KernelCoeffs<T> kc;
+  GridGeom g;
+  const cplx_t<T>* c_in;    // type 1 strengths (ntr*M)
+  cplx_t<T>* c_out;         // type 2 output (ntr*M)
+  cplx_t<T>* fw;            // fine grids (ntr*Nf), type 1 output
+  const cplx_t<T>* fw_in;   // type 2 input grid
+  int ntr;
+  int M;
+};
+
+// Cells of one subproblem tile: the bin plus the ns-1 cells its points
+// reach beyond it along each axis.
+inline size_t tile_cells(int dim, int ns, const int bs[3]) {
+  size_t n = (size_t)(bs[0] + ns - 1);
+  if (dim > 1) n *= (size_t)(bs[1] + ns - 1);
+  if (dim > 2) n *= (size_t)(bs[2] + ns - 1);
+  return n;
+}
+
+}  // namespace cfg

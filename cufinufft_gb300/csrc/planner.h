@@ -1,0 +1,45 @@
+// planner.h -- host-side plan arithmetic (no device code).
+#pragma once
+
+#include <vector>
+
+#include "kernels.h"
+
+namespace cfg {
+
+struct SpreaderParams {
+  int ns;
+  double beta;     // ES_beta in plan precision, widened to double
+  double c;        // ES_c in plan precision, widened to double
+  double upsampfac;
+};
+
+// Kernel width and ES parameters from the tolerance, restating
+// setup_spreader (contrib/spreadinterp.cpp:6-67) for the FP32 (single=true)
+// or FP64 build.  Returns 0, the warning 1 (tolerance below machine epsilon
+// or width clipped to 16), or the errors 7 / 8.
+int setup_spreader(double tol, double upsampfac, int kerevalmeth, bool single, SpreaderParams* sp);
+
+// contrib/utils.cpp:3-22 and contrib/common.cpp:24-37.
+int next235beven(int n, int b);
+int set_nf_type12(int ms, double upsampfac, int ns, int gpu_method, int bs);
+
+// n-point Gauss-Legendre rule on [-1,1] by Newton iteration on the Legendre
+// three-term recurrence; nodes in decreasing order.
+void gauss_legendre(int n, double* x, double* w);
+
+// Quadrature nodes/values for the kernel's Fourier series
+// (contrib/common.cpp:84-96): q = floor(2 + 1.5 ns) nodes z_n on (0, ns/2),
+// f_n = (ns/2) w_n phi(z_n).
+void fseries_nodes(const SpreaderParams& sp, FseriesNodes* out);
+
+// ES kernel value phi(x) in FP64.
+double es_kernel(double x, const SpreaderParams& sp);
+
+// Piecewise-polynomial fit of the kernel (kerevalmeth 1): for tap j and
+// offset d in [0,1), phi(d - ns/2 + j) ~ sum_k a_k z^(deg-k), z = 2d-1.
+// Coefficients are returned row-major [k][j], highest degree first, fitted
+// by Chebyshev interpolation in long double.
+std::vector<double> horner_fit(const SpreaderParams& sp, int degree);
+
+}  // namespace cfg

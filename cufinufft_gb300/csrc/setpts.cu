@@ -1,0 +1,256 @@
+// setpts.cu -- bin sort of the nonuniform points (the setpts stage).
+//
+// The reference sorts in four launches per call (src/2d/spread2d_wrapper.cu:
+// 386-613): CalcBinSize_noghost (per-point bin + atomic rank), a Thrust
+// exclusive scan, CalcInvertofGlobalSortIdx (scatter of the permutation),
+// then CalcSubProb / inclusive scan / MapBintoSubProb for the subproblem
+// method.  Here:
+//   * k_bin_count places every point on the fine grid (place_coord) and ranks
+//     it inside its bin with warp-aggregated atomics (one atomic per distinct
+//     bin in a warp, so clustered points do not serialise on one counter);
+//   * a three-phase block scan produces the bin starts and the subproblem
+//     starts (mode 1 scans ceil(count/maxsub) directly);
+//   * k_permute writes the sorted structure-of-arrays copy the spread and
+//     interp kernels stream: caller index, first tap and offset per axis;
+//   * k_sub_to_bin maps subproblems to bins by binary search (one thread per
+//     subproblem, balanced even when one bin holds most of the points).
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace cfg {
+
+constexpr int kPlaceThreads = 256;
+
+template <typename T>
+__device__ __forceinline__ int point_bin(const PlaceArgs<T>& a, int i, int i0[3], T d[3]) {
+  int b = 0, mul = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (k < a.dim) {
+      place_coord<T>(a.x[k][i], a.ax[k], i0[k], d[k]);
+      b += mul * (i0[k] / a.bs[k]);
+      mul *= a.nb[k];
+    }
+  }
+  return b;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPlaceThreads) k_bin_count(PlaceArgs<T> a) {
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  // warp-uniform trip count so the warp stays converged for __match_any_sync
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < a.M; base += stride) {
+    const long long ii = base + threadIdx.x;
+    const bool active = ii < a.M;
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!active) continue;
+    const int i = (int)ii;
+    int i0[3];
+    T d[3];
+    const int b = point_bin(a, i, i0, d);
+    const unsigned peers = __match_any_sync(act, b);
+    const int leader = __ffs(peers) - 1;
+    int first = 0;
+    if (lane == leader) first = atomicAdd(&a.count[b], __popc(peers));
+    first = __shfl_sync(peers, first, leader);
+    a.rank[i] = first + __popc(peers & ((1u << lane) - 1u));
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPlaceThreads) k_permute(PlaceArgs<T> a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += gridDim.x * blockDim.x) {
+    int i0[3];
+    T d[3];
+    const int b = point_bin(a, i, i0, d);
+    const int pos = a.start[b] + a.rank[i];
+    a.idx[pos] = i;
+    for (int k = 0; k < 3; ++k) {
+      if (k < a.dim) {
+        a.i0[k][pos] = i0[k];
+        a.d[k][pos] = d[k];
+      }
+    }
+  }
+}
+
+// gpu_sort = 0 with method 1 keeps the caller's order (reference "GM",
+// TrivialGlobalSortIdx, src/precision_independent.cu:98-105).
+template <typename T>
+__global__ void __launch_bounds__(kPlaceThreads) k_place_unsorted(PlaceArgs<T> a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += gridDim.x * blockDim.x) {
+    a.idx[i] = i;
+    for (int k = 0; k < 3; ++k) {
+      if (k < a.dim) {
+        int i0;
+        T d;
+        place_coord<T>(a.x[k][i], a.ax[k], i0, d);
+        a.i0[k][i] = i0;
+        a.d[k][i] = d;
+      }
+    }
+  }
+}
+
+static int place_grid(int M) {
+  long long b = ((long long)M + kPlaceThreads - 1) / kPlaceThreads;
+  if (b > 152LL * 64) b = 152LL * 64;
+  return b < 1 ? 1 : (int)b;
+}
+
+template <typename T> cudaError_t launch_bin_count(const PlaceArgs<T>& a, cudaStream_t s) {
+  if (a.M == 0) return cudaSuccess;
+  k_bin_count<T><<<place_grid(a.M), kPlaceThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+template <typename T> cudaError_t launch_permute(const PlaceArgs<T>& a, cudaStream_t s) {
+  if (a.M == 0) return cudaSuccess;
+  k_permute<T><<<place_grid(a.M), kPlaceThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+template <typename T> cudaError_t launch_place_unsorted(const PlaceArgs<T>& a, cudaStream_t s) {
+  if (a.M == 0) return cudaSuccess;
+  k_place_unsorted<T><<<place_grid(a.M), kPlaceThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_bin_count<float>(const PlaceArgs<float>&, cudaStream_t);
+template cudaError_t launch_bin_count<double>(const PlaceArgs<double>&, cudaStream_t);
+template cudaError_t launch_permute<float>(const PlaceArgs<float>&, cudaStream_t);
+template cudaError_t launch_permute<double>(const PlaceArgs<double>&, cudaStream_t);
+template cudaError_t launch_place_unsorted<float>(const PlaceArgs<float>&, cudaStream_t);
+template cudaError_t launch_place_unsorted<double>(const PlaceArgs<double>&, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Exclusive scan: 1024 threads x 4 items per block; block totals are scanned
+// by one block (up to 4096 blocks, i.e. 16.7M entries), then added back.
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int kScanMaxBlocks = 4096;
+
+__device__ __forceinline__ int scan_load(const int* in, int i, int n, int mode, int div) {
+  if (i >= n) return 0;
+  int v = in[i];
+  return mode == 1 ? (v + div - 1) / div : v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+__device__ __forceinline__ int block_exclusive_scan(int v, int& excl) {
+  __shared__ int warp_tot[kScanThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int n = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += n;
+  }
+  if (lane == 31) warp_tot[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    int t = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+    int ti = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int n = __shfl_up_sync(0xffffffffu, ti, o);
+      if (lane >= o) ti += n;
+    }
+    warp_tot[lane] = ti - t;  // exclusive warp offsets
+  }
+  __syncthreads();
+  excl = warp_tot[w] + incl - v;
+  __shared__ int tot;
+  if (threadIdx.x == blockDim.x - 1) tot = excl + v;  // inclusive sum of the last thread
+  __syncthreads();
+  const int total = tot;
+  __syncthreads();
+  return total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_partial(const int* in, int n, int mode, int div,
+                                                              int* partial) {
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) s += scan_load(in, base + k, n, mode, div);
+  int excl;
+  int total = block_exclusive_scan(s, excl);
+  if (threadIdx.x == 0) partial[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_partials(int* partial, int nblocks) {
+  // one block: exclusive scan of nblocks (<= 4096) partial sums in place
+  int v[kScanItems];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int i = threadIdx.x * kScanItems + k;
+    v[k] = i < nblocks ? partial[i] : 0;
+    s += v[k];
+  }
+  int excl;
+  block_exclusive_scan(s, excl);
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    int i = threadIdx.x * kScanItems + k;
+    if (i < nblocks) partial[i] = excl;
+    excl += v[k];
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_final(const int* in, int n, int mode, int div,
+                                                            const int* partial, int* out) {
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  int v[kScanItems];
+  int s = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = scan_load(in, base + k, n, mode, div);
+    s += v[k];
+  }
+  int excl;
+  int total = block_exclusive_scan(s, excl);
+  excl += partial[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < n) out[base + k] = excl;
+    excl += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = partial[blockIdx.x] + total;
+}
+
+int scan_tmp_ints(int n) {
+  int nb = (n + kScanTile - 1) / kScanTile;
+  return nb < 1 ? 1 : nb;
+}
+
+cudaError_t launch_scan(const int* in, int* out, int n, int mode, int div, int* tmp, cudaStream_t s) {
+  if (n <= 0) return cudaMemsetAsync(out, 0, sizeof(int), s);
+  int nb = scan_tmp_ints(n);
+  if (nb > kScanMaxBlocks) return cudaErrorInvalidValue;
+  k_scan_partial<<<nb, kScanThreads, 0, s>>>(in, n, mode, div, tmp);
+  k_scan_partials<<<1, kScanThreads, 0, s>>>(tmp, nb);
+  k_scan_final<<<nb, kScanThreads, 0, s>>>(in, n, mode, div, tmp, out);
+  return cudaGetLastError();
+}
+
+__global__ void k_sub_to_bin(const int* sub_start, int nbins, int nsub, int* sub_to_bin) {
+  for (int sidx = blockIdx.x * blockDim.x + threadIdx.x; sidx < nsub; sidx += gridDim.x * blockDim.x) {
+    // largest b with sub_start[b] <= sidx
+    int lo = 0, hi = nbins;  // invariant: sub_start[lo] <= sidx < sub_start[hi]
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (sub_start[mid] <= sidx) lo = mid;
+      else hi = mid;
+    }
+    sub_to_bin[sidx] = lo;
+  }
+}
+
+cudaError_t launch_sub_to_bin(const int* sub_start, int nbins, int nsub, int* sub_to_bin, cudaStream_t s) {
+  if (nsub <= 0) return cudaSuccess;
+  k_sub_to_bin<<<place_grid(nsub), kPlaceThreads, 0, s>>>(sub_start, nbins, nsub, sub_to_bin);
+  return cudaGetLastError();
+}
+
+}  // namespace cfg

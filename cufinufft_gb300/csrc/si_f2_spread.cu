@@ -1,0 +1,6 @@
+// spread kernels for float plans in 2D (all kernel widths 2..16).
+#include "spreadinterp.cuh"
+
+namespace cfg {
+template cudaError_t spread_dim<float, 2>(int, int, const SpreadArgs<float>&, cudaStream_t);
+}  // namespace cfg

@@ -1,0 +1,367 @@
+// spreadinterp.cuh -- spreading (type 1) and interpolation (type 2) kernels.
+//
+// Method 1 ("NU-point driven", src/2d/spreadinterp2d.cu:16-98 and :516-593
+// of the reference): one thread per (bin-sorted) point; spreading adds its
+// ns^d taps straight into the fine grid with vector reductions, interpolation
+// gathers them.  Method 2 ("subproblem", src/2d/spreadinterp2d.cu:152-312 and
+// :596-745): one block per subproblem (<= maxsub points of one bin) works in a
+// shared-memory tile that covers the bin plus the ns-1 cells its points reach
+// beyond it; spreading accumulates with shared atomics and flushes the tile
+// once, interpolation loads the tile once and gathers from it.
+//
+// Differences from the reference kernels, all result-preserving:
+//   * points are read from the plan's sorted SoA copy (first tap + offset in
+//     [0,1), see place_coord), not re-rescaled from the caller's arrays;
+//   * each thread evaluates its kernel rows once and reuses them for every
+//     transform of the batch (the reference launches once per transform);
+//   * FP32 plans evaluate the kernel in FP32 (the reference promotes the
+//     FP32 build's kernel to FP64, src/cuspreadinterp.h:15);
+//   * the tile is bs + ns - 1 wide (the reference pads 2*ceil(ns/2)), and the
+//     flush skips cells no point touched.
+#pragma once
+
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace cfg {
+
+constexpr int kSpreadThreads = 256;
+
+// ---------------------------------------------------------------------------
+// Method 1: NU-point driven spread.
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_spread_gm(SpreadArgs<T> a) {
+  using C = cplx_t<T>;
+  constexpr int HD = horner_degree<T>(NS);
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.M; p += gridDim.x * blockDim.x) {
+    T k1[NS], k2[NS];
+    int xs[NS];
+    const int i1 = a.pts.i0[0][p];
+    kernel_row<T, NS, HD>(a.pts.d[0][p], a.kc, k1);
+#pragma unroll
+    for (int j = 0; j < NS; ++j) xs[j] = wrap_idx(i1 + j, nf0);
+    int i2 = 0, i3 = 0;
+    if (DIM > 1) { i2 = a.pts.i0[1][p]; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
+    T d3 = T(0);
+    if (DIM > 2) { i3 = a.pts.i0[2][p]; d3 = a.pts.d[2][p]; }
+    const int src = a.pts.idx[p];
+    for (int t = 0; t < a.ntr; ++t) {
+      const C v = a.c_in[(size_t)t * a.M + src];
+      C* base = a.fw + (size_t)t * a.g.Nf;
+#pragma unroll 1
+      for (int dz = 0; dz < NZ; ++dz) {
+        const int iz = DIM > 2 ? wrap_idx(i3 + dz, nf2) : 0;
+        const T kz = DIM > 2 ? kernel_tap<T, NS, HD>(d3, dz, a.kc) : T(1);
+#pragma unroll
+        for (int dy = 0; dy < NY; ++dy) {
+          const int iy = DIM > 1 ? wrap_idx(i2 + dy, nf1) : 0;
+          T kyz = T(1);
+          if (DIM > 1) kyz = k2[dy];
+          if (DIM > 2) kyz *= kz;
+          const T vr = v.x * kyz, vi = v.y * kyz;
+          C* row = base + ((size_t)iz * nf1 + iy) * nf0;
+#pragma unroll
+          for (int dx = 0; dx < NS; ++dx) red_add(row + xs[dx], vr * k1[dx], vi * k1[dx]);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Method 2: shared-memory subproblem spread.  grid = (nsub, ntr).
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_spread_sm(SpreadArgs<T> a) {
+  using C = cplx_t<T>;
+  constexpr int HD = horner_degree<T>(NS);
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tile = reinterpret_cast<C*>(smem_raw);
+
+  const BinTables& bt = a.bins;
+  const int sub = blockIdx.x, t = blockIdx.y;
+  const int b = bt.sub_to_bin[sub];
+  const int js = sub - bt.sub_start[b];
+  const int p0 = bt.start[b] + js * bt.maxsub;
+  const int np = min(bt.maxsub, bt.count[b] - js * bt.maxsub);
+  const int bx = b % bt.nb[0];
+  const int by = (b / bt.nb[0]) % bt.nb[1];
+  const int bz = b / (bt.nb[0] * bt.nb[1]);
+  const int ox = bx * bt.bs[0], oy = by * bt.bs[1], oz = bz * bt.bs[2];
+  const int TX = bt.bs[0] + NS - 1;
+  const int TY = DIM > 1 ? bt.bs[1] + NS - 1 : 1;
+  const int TZ = DIM > 2 ? bt.bs[2] + NS - 1 : 1;
+  const int ntile = TX * TY * TZ;
+
+  for (int i = threadIdx.x; i < ntile; i += blockDim.x) {
+    tile[i].x = T(0);
+    tile[i].y = T(0);
+  }
+  __syncthreads();
+
+  const C* cin = a.c_in + (size_t)t * a.M;
+  for (int p = p0 + threadIdx.x; p < p0 + np; p += blockDim.x) {
+    T k1[NS], k2[NS];
+    const int lx = a.pts.i0[0][p] - ox;
+    kernel_row<T, NS, HD>(a.pts.d[0][p], a.kc, k1);
+    int ly = 0, lz = 0;
+    if (DIM > 1) { ly = a.pts.i0[1][p] - oy; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
+    T d3 = T(0);
+    if (DIM > 2) { lz = a.pts.i0[2][p] - oz; d3 = a.pts.d[2][p]; }
+    const C v = cin[a.pts.idx[p]];
+#pragma unroll 1
+    for (int dz = 0; dz < NZ; ++dz) {
+      const T kz = DIM > 2 ? kernel_tap<T, NS, HD>(d3, dz, a.kc) : T(1);
+#pragma unroll
+      for (int dy = 0; dy < NY; ++dy) {
+        T kyz = T(1);
+        if (DIM > 1) kyz = k2[dy];
+        if (DIM > 2) kyz *= kz;
+        const T vr = v.x * kyz, vi = v.y * kyz;
+        C* row = tile + ((lz + dz) * TY + (ly + dy)) * TX + lx;
+#pragma unroll
+        for (int dx = 0; dx < NS; ++dx) smem_add(row + dx, vr * k1[dx], vi * k1[dx]);
+      }
+    }
+  }
+  __syncthreads();
+
+  C* base = a.fw + (size_t)t * a.g.Nf;
+  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
+  for (int i = threadIdx.x; i < ntile; i += blockDim.x) {
+    const C v = tile[i];
+    if (v.x == T(0) && v.y == T(0)) continue;
+    const int ix = i % TX;
+    const int iy = (i / TX) % TY;
+    const int iz = i / (TX * TY);
+    int gx = ox + ix, gy = oy + iy, gz = oz + iz;
+    while (gx >= nf0) gx -= nf0;
+    while (gy >= nf1) gy -= nf1;
+    while (gz >= nf2) gz -= nf2;
+    red_add(base + ((size_t)gz * nf1 + gy) * nf0 + gx, v.x, v.y);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Method 1: NU-point driven interpolation (gather).
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_interp_gm(SpreadArgs<T> a) {
+  using C = cplx_t<T>;
+  constexpr int HD = horner_degree<T>(NS);
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.M; p += gridDim.x * blockDim.x) {
+    T k1[NS], k2[NS];
+    int xs[NS];
+    const int i1 = a.pts.i0[0][p];
+    kernel_row<T, NS, HD>(a.pts.d[0][p], a.kc, k1);
+#pragma unroll
+    for (int j = 0; j < NS; ++j) xs[j] = wrap_idx(i1 + j, nf0);
+    int i2 = 0, i3 = 0;
+    if (DIM > 1) { i2 = a.pts.i0[1][p]; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
+    T d3 = T(0);
+    if (DIM > 2) { i3 = a.pts.i0[2][p]; d3 = a.pts.d[2][p]; }
+    const int dst = a.pts.idx[p];
+    for (int t = 0; t < a.ntr; ++t) {
+      const C* base = a.fw_in + (size_t)t * a.g.Nf;
+      T ar = T(0), ai = T(0);
+#pragma unroll 1
+      for (int dz = 0; dz < NZ; ++dz) {
+        const int iz = DIM > 2 ? wrap_idx(i3 + dz, nf2) : 0;
+        const T kz = DIM > 2 ? kernel_tap<T, NS, HD>(d3, dz, a.kc) : T(1);
+#pragma unroll
+        for (int dy = 0; dy < NY; ++dy) {
+          const int iy = DIM > 1 ? wrap_idx(i2 + dy, nf1) : 0;
+          const C* row = base + ((size_t)iz * nf1 + iy) * nf0;
+          T rr = T(0), ri = T(0);
+#pragma unroll
+          for (int dx = 0; dx < NS; ++dx) {
+            const C g = __ldg(row + xs[dx]);
+            rr = fma_rn(g.x, k1[dx], rr);
+            ri = fma_rn(g.y, k1[dx], ri);
+          }
+          T kyz = T(1);
+          if (DIM > 1) kyz = k2[dy];
+          if (DIM > 2) kyz *= kz;
+          ar = fma_rn(rr, kyz, ar);
+          ai = fma_rn(ri, kyz, ai);
+        }
+      }
+      C out;
+      out.x = ar;
+      out.y = ai;
+      a.c_out[(size_t)t * a.M + dst] = out;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Method 2: shared-memory subproblem interpolation.  grid = (nsub, ntr).
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_interp_sm(SpreadArgs<T> a) {
+  using C = cplx_t<T>;
+  constexpr int HD = horner_degree<T>(NS);
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tile = reinterpret_cast<C*>(smem_raw);
+
+  const BinTables& bt = a.bins;
+  const int sub = blockIdx.x, t = blockIdx.y;
+  const int b = bt.sub_to_bin[sub];
+  const int js = sub - bt.sub_start[b];
+  const int p0 = bt.start[b] + js * bt.maxsub;
+  const int np = min(bt.maxsub, bt.count[b] - js * bt.maxsub);
+  const int bx = b % bt.nb[0];
+  const int by = (b / bt.nb[0]) % bt.nb[1];
+  const int bz = b / (bt.nb[0] * bt.nb[1]);
+  const int ox = bx * bt.bs[0], oy = by * bt.bs[1], oz = bz * bt.bs[2];
+  const int TX = bt.bs[0] + NS - 1;
+  const int TY = DIM > 1 ? bt.bs[1] + NS - 1 : 1;
+  const int TZ = DIM > 2 ? bt.bs[2] + NS - 1 : 1;
+  const int ntile = TX * TY * TZ;
+  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
+
+  const C* base = a.fw_in + (size_t)t * a.g.Nf;
+  for (int i = threadIdx.x; i < ntile; i += blockDim.x) {
+    const int ix = i % TX;
+    const int iy = (i / TX) % TY;
+    const int iz = i / (TX * TY);
+    int gx = ox + ix, gy = oy + iy, gz = oz + iz;
+    while (gx >= nf0) gx -= nf0;
+    while (gy >= nf1) gy -= nf1;
+    while (gz >= nf2) gz -= nf2;
+    tile[i] = __ldg(base + ((size_t)gz * nf1 + gy) * nf0 + gx);
+  }
+  __syncthreads();
+
+  for (int p = p0 + threadIdx.x; p < p0 + np; p += blockDim.x) {
+    T k1[NS], k2[NS];
+    const int lx = a.pts.i0[0][p] - ox;
+    kernel_row<T, NS, HD>(a.pts.d[0][p], a.kc, k1);
+    int ly = 0, lz = 0;
+    if (DIM > 1) { ly = a.pts.i0[1][p] - oy; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
+    T d3 = T(0);
+    if (DIM > 2) { lz = a.pts.i0[2][p] - oz; d3 = a.pts.d[2][p]; }
+    T ar = T(0), ai = T(0);
+#pragma unroll 1
+    for (int dz = 0; dz < NZ; ++dz) {
+      const T kz = DIM > 2 ? kernel_tap<T, NS, HD>(d3, dz, a.kc) : T(1);
+#pragma unroll
+      for (int dy = 0; dy < NY; ++dy) {
+        const C* row = tile + ((lz + dz) * TY + (ly + dy)) * TX + lx;
+        T rr = T(0), ri = T(0);
+#pragma unroll
+        for (int dx = 0; dx < NS; ++dx) {
+          const C g = row[dx];
+          rr = fma_rn(g.x, k1[dx], rr);
+          ri = fma_rn(g.y, k1[dx], ri);
+        }
+        T kyz = T(1);
+        if (DIM > 1) kyz = k2[dy];
+        if (DIM > 2) kyz *= kz;
+        ar = fma_rn(rr, kyz, ar);
+        ai = fma_rn(ri, kyz, ai);
+      }
+    }
+    C out;
+    out.x = ar;
+    out.y = ai;
+    a.c_out[(size_t)t * a.M + a.pts.idx[p]] = out;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers, instantiated per (T, DIM) in si_*.cu.
+
+inline int grid_for(long long n, int threads) {
+  long long b = (n + threads - 1) / threads;
+  const long long cap = 152LL * 32;  // grid-stride beyond this
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+template <typename T, int DIM>
+size_t tile_bytes(int ns, const BinTables& bt) {
+  return tile_cells(DIM, ns, bt.bs) * sizeof(cplx_t<T>);
+}
+
+template <typename K>
+cudaError_t prepare_smem(K kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <typename T, int DIM, int NS>
+cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
+  if (a.M == 0) return cudaSuccess;
+  if (method == 1) {
+    k_spread_gm<T, DIM, NS><<<grid_for(a.M, kSpreadThreads), kSpreadThreads, 0, s>>>(a);
+  } else {
+    if (a.bins.nsub == 0) return cudaSuccess;
+    size_t sm = tile_bytes<T, DIM>(NS, a.bins);
+    cudaError_t e = prepare_smem(k_spread_sm<T, DIM, NS>, sm);
+    if (e != cudaSuccess) return e;
+    dim3 grid(a.bins.nsub, a.ntr);
+    k_spread_sm<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+template <typename T, int DIM, int NS>
+cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
+  if (a.M == 0) return cudaSuccess;
+  if (method == 1) {
+    k_interp_gm<T, DIM, NS><<<grid_for(a.M, kSpreadThreads), kSpreadThreads, 0, s>>>(a);
+  } else {
+    if (a.bins.nsub == 0) return cudaSuccess;
+    size_t sm = tile_bytes<T, DIM>(NS, a.bins);
+    cudaError_t e = prepare_smem(k_interp_sm<T, DIM, NS>, sm);
+    if (e != cudaSuccess) return e;
+    dim3 grid(a.bins.nsub, a.ntr);
+    k_interp_sm<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
+  }
+  return cudaGetLastError();
+}
+
+#define CFG_NS_SWITCH(FN, T, DIM, ...)            \
+  switch (ns) {                                   \
+    case 2: return FN<T, DIM, 2>(__VA_ARGS__);    \
+    case 3: return FN<T, DIM, 3>(__VA_ARGS__);    \
+    case 4: return FN<T, DIM, 4>(__VA_ARGS__);    \
+    case 5: return FN<T, DIM, 5>(__VA_ARGS__);    \
+    case 6: return FN<T, DIM, 6>(__VA_ARGS__);    \
+    case 7: return FN<T, DIM, 7>(__VA_ARGS__);    \
+    case 8: return FN<T, DIM, 8>(__VA_ARGS__);    \
+    case 9: return FN<T, DIM, 9>(__VA_ARGS__);    \
+    case 10: return FN<T, DIM, 10>(__VA_ARGS__);  \
+    case 11: return FN<T, DIM, 11>(__VA_ARGS__);  \
+    case 12: return FN<T, DIM, 12>(__VA_ARGS__);  \
+    case 13: return FN<T, DIM, 13>(__VA_ARGS__);  \
+    case 14: return FN<T, DIM, 14>(__VA_ARGS__);  \
+    case 15: return FN<T, DIM, 15>(__VA_ARGS__);  \
+    case 16: return FN<T, DIM, 16>(__VA_ARGS__);  \
+    default: return cudaErrorInvalidValue;        \
+  }
+
+template <typename T, int DIM>
+cudaError_t spread_dim(int method, int ns, const SpreadArgs<T>& a, cudaStream_t s) {
+  CFG_NS_SWITCH(spread_ns, T, DIM, method, a, s)
+}
+
+template <typename T, int DIM>
+cudaError_t interp_dim(int method, int ns, const SpreadArgs<T>& a, cudaStream_t s) {
+  CFG_NS_SWITCH(interp_ns, T, DIM, method, a, s)
+}
+
+}  // namespace cfg

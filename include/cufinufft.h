@@ -1,0 +1,126 @@
+/* cufinufft.h -- C ABI of the GB300-native type-1/type-2 NUFFT library.
+ *
+ * Drop-in for the public interface of cuFINUFFT v1.3: the ten entry points
+ * below have the reference's names, argument lists and meanings
+ * (include/cufinufft_eitherprec.h:311-324 of the reference, documented in its
+ * docs/cppdoc.md), and cufinufft_opts is byte-identical (cufinufft_opts.h).
+ * "cufinufft_*" is the FP64 library, "cufinufftf_*" the FP32 one.
+ *
+ * Semantics kept from the reference:
+ *   - plans are opaque pointers; one plan is not re-entrant, distinct plans
+ *     may be used from distinct host threads;
+ *   - x, y, z, c, fk are DEVICE pointers owned by the caller; nmodes[0] is
+ *     the fastest (x) dimension; fk is in CMCL order, k = -N/2..(N-1)/2 with
+ *     k1 fastest, then the transform index; c is transform-major;
+ *   - iflag >= 0 selects exp(+i k.x), otherwise exp(-i k.x); sums are not
+ *     normalised; points lie in [-pi, pi) (one period either side,
+ *     [-3pi, 3pi), is folded in);
+ *   - the stages may be repeated: 1234, 123334 and 1232334 are valid;
+ *   - return value 0 = success; makeplan swallows the tolerance warning (1).
+ * Differences, by design:
+ *   - setpts copies the bin-sorted, rescaled points into plan memory, so the
+ *     coordinate arrays may be freed or reused after setpts returns;
+ *   - CUDA and cuFFT failures are returned as error codes (the reference
+ *     calls exit() inside the library);
+ *   - work is queued on a plan-owned blocking stream (ordered after the
+ *     legacy default stream), or on the stream given to *_set_stream.
+ */
+#ifndef CUFINUFFT_GB300_H
+#define CUFINUFFT_GB300_H
+
+#include <cuComplex.h>
+#include <cuda_runtime_api.h>
+
+#include "cufinufft_opts.h"
+
+/* Return codes.  1..9 are the reference's (contrib/utils.h:28-36 and the
+ * method checks in src/2d/spread2d_wrapper.cu:155); 10.. are this library's. */
+#define CUFINUFFT_WARN_EPS_TOO_SMALL 1
+#define CUFINUFFT_ERR_GENERIC 1        /* also: type 3, bad binsize, NULL plan */
+#define CUFINUFFT_ERR_METHOD 2         /* gpu_method not valid for this dim/type */
+#define CUFINUFFT_ERR_UPSAMPFAC_TOO_SMALL 7
+#define CUFINUFFT_ERR_HORNER_WRONG_BETA 8
+#define CUFINUFFT_ERR_NDATA_NOTVALID 9
+#define CUFINUFFT_ERR_CUDA 10          /* a CUDA runtime call failed        */
+#define CUFINUFFT_ERR_CUFFT 11         /* a cuFFT call failed               */
+#define CUFINUFFT_ERR_ALLOC 12         /* device allocation failed          */
+#define CUFINUFFT_ERR_ARG 13           /* invalid argument (sizes, pointers) */
+#define CUFINUFFT_ERR_SHMEM 14         /* bin tile exceeds shared memory    */
+
+typedef struct cufinufft_plan_s* cufinufft_plan;
+typedef struct cufinufftf_plan_s* cufinufftf_plan;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Fill *opts with the defaults for (type, dim).  Replaces
+ * cufinufft[f]_default_opts, src/cufinufft.cu:639-730. */
+int cufinufft_default_opts(int type, int dim, cufinufft_opts* opts);
+int cufinufftf_default_opts(int type, int dim, cufinufft_opts* opts);
+
+/* Make a plan.  Replaces CUFINUFFT_MAKEPLAN, src/cufinufft.cu:78-273
+ * (include/cufinufft_eitherprec.h:313-315).  opts may be NULL (defaults on
+ * device 0).  maxbatchsize 0 picks min(ntransf, 8). */
+int cufinufft_makeplan(int type, int dim, int* nmodes, int iflag, int ntransf,
+                       double tol, int maxbatchsize, cufinufft_plan* plan,
+                       cufinufft_opts* opts);
+int cufinufftf_makeplan(int type, int dim, int* nmodes, int iflag, int ntransf,
+                        float tol, int maxbatchsize, cufinufftf_plan* plan,
+                        cufinufft_opts* opts);
+
+/* Set the M nonuniform points (device arrays; y unused in 1D, z unused in
+ * 1D/2D; N, s, t, u are the type-3 arguments and are ignored).  Replaces
+ * CUFINUFFT_SETPTS, src/cufinufft.cu:275-493. */
+int cufinufft_setpts(int M, double* x, double* y, double* z, int N, double* s,
+                     double* t, double* u, cufinufft_plan plan);
+int cufinufftf_setpts(int M, float* x, float* y, float* z, int N, float* s,
+                      float* t, float* u, cufinufftf_plan plan);
+
+/* Run ntransf transforms: type 1 reads c (ntransf*M) and writes fk
+ * (ntransf*N1*N2*N3); type 2 reads fk and writes c.  Replaces
+ * CUFINUFFT_EXECUTE, src/cufinufft.cu:495-569. */
+int cufinufft_execute(cuDoubleComplex* c, cuDoubleComplex* fk,
+                      cufinufft_plan plan);
+int cufinufftf_execute(cuFloatComplex* c, cuFloatComplex* fk,
+                       cufinufftf_plan plan);
+
+/* Free a plan and its device memory.  Replaces CUFINUFFT_DESTROY,
+ * src/cufinufft.cu:571-637.  Returns 1 for a NULL plan, as the reference. */
+int cufinufft_destroy(cufinufft_plan plan);
+int cufinufftf_destroy(cufinufftf_plan plan);
+
+/* ---- extensions (no counterpart in the reference) ----------------------- */
+
+/* Queue all later work of this plan on `stream` (NULL restores the plan's
+ * own stream).  The reference has no stream argument; this lets a caller
+ * order a plan with its own work and capture execute() in a CUDA graph. */
+int cufinufft_set_stream(cufinufft_plan plan, cudaStream_t stream);
+int cufinufftf_set_stream(cufinufftf_plan plan, cudaStream_t stream);
+
+/* Plan facts for callers and tools: fine-grid sizes, kernel width, the
+ * method actually run, total bins and subproblems of the last setpts. */
+typedef struct cufinufft_plan_info {
+  int type, dim, ms, mt, mu, nf1, nf2, nf3, ns, M, ntransf, maxbatchsize;
+  int method, sort, binsizex, binsizey, binsizez, nbins, nsubprob, kerevalmeth;
+  double beta, es_c;
+} cufinufft_plan_info;
+int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info);
+int cufinufftf_get_info(cufinufftf_plan plan, cufinufft_plan_info* info);
+
+/* Stage timing.  With timing on, execute() records CUDA events around its
+ * three stages on the plan stream; stage_times() waits for them and returns
+ * the accumulated milliseconds ms[0] = spread (type 1) or interp (type 2)
+ * kernel, ms[1] = cuFFT, ms[2] = deconvolve (type 1, with the grid clear)
+ * or amplify (type 2), plus the number of batches timed; reset != 0 clears
+ * the totals. */
+int cufinufft_set_timing(cufinufft_plan plan, int on);
+int cufinufftf_set_timing(cufinufftf_plan plan, int on);
+int cufinufft_stage_times(cufinufft_plan plan, double* ms, long long* batches, int reset);
+int cufinufftf_stage_times(cufinufftf_plan plan, double* ms, long long* batches, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUFINUFFT_GB300_H */

@@ -169,9 +169,17 @@ class OraclePlan:
     def _modes3(self):
         return list(self.modes) + [1] * (3 - self.dim)
 
+    fft_workers = 0  # > 0: scipy.fft with that many threads (CPU baseline timing)
+
     def _fft(self, fw: np.ndarray) -> np.ndarray:
         axes = tuple(range(-self.dim, 0))
         # cuFFT's CUFFT_INVERSE (iflag>=0) is the unnormalised +i transform.
+        if self.fft_workers > 0:
+            import scipy.fft as sf
+            if self.iflag > 0:
+                return sf.ifftn(fw, axes=axes, norm="forward", workers=self.fft_workers,
+                                overwrite_x=True)
+            return sf.fftn(fw, axes=axes, workers=self.fft_workers, overwrite_x=True)
         if self.iflag > 0:
             return np.fft.ifftn(fw, axes=axes, norm="forward")
         return np.fft.fftn(fw, axes=axes)

@@ -1,0 +1,252 @@
+"""The reference's own Python tests, restated for this library's interface
+(python/cufinufft/tests/test_basic.py, test_error_checks.py of cuFINUFFT
+v1.3), plus the stage-repetition and error-return behaviour of the C ABI
+(docs/cppdoc.md:3-8 of the reference)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests import nufft_cases as NC
+
+pytestmark = pytest.mark.gpu
+
+
+def _gen_nu_pts(M, dim=3, seed=0):
+    # python/cufinufft/tests/utils.py:26-30
+    np.random.seed(seed)
+    return np.random.uniform(-np.pi, np.pi, (dim, M)).astype(np.float64)
+
+
+def _gen_uniform_data(shape, seed=0):
+    np.random.seed(seed)
+    fk = np.random.standard_normal(shape + (2,))
+    return fk.astype(np.float64).view(np.complex128)[..., 0]
+
+
+def _gen_nonuniform_data(M, seed=0):
+    np.random.seed(seed)
+    return np.random.standard_normal(2 * M).astype(np.float64).view(np.complex128)
+
+
+def _make_grid(shape):
+    dim = len(shape)
+    shape = (1,) * (3 - dim) + shape
+    grids = [np.arange(-(N // 2), (N + 1) // 2) for N in shape]
+    x, y, z = np.meshgrid(*grids, indexing='ij')
+    return np.stack((x, y, z))
+
+
+def _direct_type1(c, k, shape, ind):
+    grid = _make_grid(shape)
+    phase = k.T @ grid.reshape((3, -1))[:, ind]
+    return np.sum(c * np.exp(1j * phase))
+
+
+def _direct_type2(fk, k):
+    grid = _make_grid(fk.shape)
+    phase = k @ grid.reshape((3, -1))
+    return np.sum(fk.ravel() * np.exp(-1j * phase))
+
+
+def _cuda(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_type1(dtype, shape=(16, 16, 16), M=4096, tol=1e-3):
+    import torch
+
+    from cufinufft_gb300 import cufinufft
+    complex_dtype = np.complex64 if dtype == np.float32 else np.complex128
+    k = _gen_nu_pts(M, dim=len(shape)).astype(dtype)
+    c = _gen_nonuniform_data(M).astype(complex_dtype)
+    k_gpu = _cuda(k)
+    c_gpu = _cuda(c)
+    fk_gpu = torch.zeros(shape, dtype=c_gpu.dtype, device="cuda")
+    plan = cufinufft(1, shape, eps=tol, dtype=dtype)
+    plan.set_pts(k_gpu[0], k_gpu[1], k_gpu[2])
+    plan.execute(c_gpu, fk_gpu)
+    fk = fk_gpu.cpu().numpy()
+    ind = int(0.1789 * np.prod(shape))
+    fk_target = _direct_type1(c, k, shape, ind)
+    assert np.abs(fk_target - fk.ravel()[ind]) / np.abs(fk_target) < 0.01
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_type2(dtype, shape=(16, 16, 16), M=4096, tol=1e-3):
+    import torch
+
+    from cufinufft_gb300 import cufinufft
+    complex_dtype = np.complex64 if dtype == np.float32 else np.complex128
+    k = _gen_nu_pts(M).astype(dtype)
+    fk = _gen_uniform_data(shape).astype(complex_dtype)
+    k_gpu = _cuda(k)
+    fk_gpu = _cuda(fk)
+    c_gpu = torch.zeros((M,), dtype=fk_gpu.dtype, device="cuda")
+    plan = cufinufft(2, shape, eps=tol, dtype=dtype)
+    plan.set_pts(k_gpu[0], k_gpu[1], k_gpu[2])
+    plan.execute(c_gpu, fk_gpu)
+    c = c_gpu.cpu().numpy()
+    ind = M // 2
+    c_target = _direct_type2(fk, k[:, ind])
+    assert np.abs(c_target - c[ind]) / np.abs(c_target) < 0.01
+
+
+def test_opts(shape=(8, 8, 8), M=32, tol=1e-3):
+    import torch
+
+    from cufinufft_gb300 import cufinufft
+    k = _gen_nu_pts(M, dim=len(shape)).astype(np.float32)
+    c = _gen_nonuniform_data(M).astype(np.complex64)
+    k_gpu = _cuda(k)
+    c_gpu = _cuda(c)
+    fk_gpu = torch.zeros(shape, dtype=torch.complex64, device="cuda")
+    plan = cufinufft(1, shape, eps=tol, dtype=np.float32, gpu_sort=False, gpu_maxsubprobsize=10)
+    plan.set_pts(k_gpu[0], k_gpu[1], k_gpu[2])
+    plan.execute(c_gpu, fk_gpu)
+    fk = fk_gpu.cpu().numpy()
+    ind = int(0.1789 * np.prod(shape))
+    fk_target = _direct_type1(c, k, shape, ind)
+    assert np.abs(fk_target - fk.ravel()[ind]) / np.abs(fk_target) < 0.01
+
+
+def test_set_pts_raises_on_dtype_and_size():
+    from cufinufft_gb300 import cufinufft
+    kxyz = _gen_nu_pts(4096, dim=3).astype(np.float32)
+    k_gpu = _cuda(kxyz)
+    k_wrong = _cuda(kxyz.astype(np.float64))
+    plan = cufinufft(1, (16, 16, 16), eps=1e-3, dtype=np.float32)
+    with pytest.raises(TypeError):
+        plan.set_pts(k_wrong[0], k_gpu[1], k_gpu[2])
+    with pytest.raises(TypeError):
+        plan.set_pts(k_gpu[0], k_wrong[1], k_gpu[2])
+    with pytest.raises(TypeError):
+        plan.set_pts(k_gpu[0], k_gpu[1], k_wrong[2])
+    with pytest.raises(TypeError) as err:
+        plan.set_pts(k_gpu[0], k_gpu[1][:4])
+    assert 'kx and ky must be equal' in err.value.args[0]
+    with pytest.raises(TypeError) as err:
+        plan.set_pts(k_gpu[0], k_gpu[1], k_gpu[2][:4])
+    assert 'kx and kz must be equal' in err.value.args[0]
+
+
+def test_exec_raises_on_dtype():
+    import torch
+
+    from cufinufft_gb300 import cufinufft
+    M = 4096
+    kxyz = _gen_nu_pts(M, dim=3).astype(np.float32)
+    c = _gen_nonuniform_data(M).astype(np.complex64)
+    c_gpu = _cuda(c)
+    c_wrong = _cuda(c.real.copy())
+    k_gpu = _cuda(kxyz)
+    fk_gpu = torch.zeros((16, 16, 16), dtype=torch.complex64, device="cuda")
+    fk_wrong = torch.zeros((16, 16, 16), dtype=torch.complex128, device="cuda")
+    plan = cufinufft(1, (16, 16, 16), eps=1e-3, dtype=np.float32)
+    plan.set_pts(k_gpu[0], k_gpu[1], k_gpu[2])
+    with pytest.raises(TypeError):
+        plan.execute(c_gpu, fk_wrong)
+    with pytest.raises(TypeError):
+        plan.execute(c_wrong, fk_gpu)
+
+
+def test_stage_repetition_1232334():
+    """setpts may be repeated with a new M on one plan, execute repeated."""
+    rng = np.random.default_rng(5)
+    modes = (40, 36)
+    for single in (True, False):
+        tol = 1e-5 if single else 1e-10
+        dt = np.float32 if single else np.float64
+        cdt = np.complex64 if single else np.complex128
+        import torch
+
+        from cufinufft_gb300 import cufinufft
+        plan = cufinufft(1, modes[::-1], eps=tol, dtype=dt)
+        for M in (1000, 5000, 0, 300):
+            pts = NC.points(rng, 2, M, dtype=dt, edges=M >= 8)
+            plan.set_pts(*[_cuda(p) for p in pts[::-1]])
+            for _ in range(2):
+                c = NC.strengths(rng, M).astype(cdt)
+                fk = torch.zeros(modes[::-1], dtype=_cuda(c).dtype, device="cuda")
+                plan.execute(_cuda(c), fk)
+                out = fk.cpu().numpy()
+                if M == 0:
+                    assert np.all(out == 0)
+                    continue
+                ref = NC.oracle_nufft(1, modes, [p.astype(np.float64) for p in pts],
+                                      c.astype(np.complex128), tol, single)
+                err = np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
+                assert err < (2e-5 if single else 1e-10)
+
+
+def _raw(single):
+    from cufinufft_gb300 import _cufinufft as L
+    if single:
+        return L._make_planf, L._set_ptsf, L._exec_planf, L._destroy_planf
+    return L._make_plan, L._set_pts, L._exec_plan, L._destroy_plan
+
+
+def test_c_abi_error_returns():
+    import torch
+
+    from cufinufft_gb300 import _cufinufft as L
+    mk, sp, ex, de = _raw(True)
+    nmodes = (ctypes.c_int * 3)(16, 16, 16)
+    # type 3 is reserved: makeplan returns 1 (src/cufinufft.cu:533-536)
+    plan = ctypes.c_void_p(None)
+    assert mk(3, 3, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), None) == 1
+    assert de(plan) == 0
+    # a method the dimension does not offer: execute returns 2
+    # (src/3d/spread3d_wrapper.cu:155-157)
+    opts = L.NufftOpts()
+    L._default_optsf(1, 3, opts)
+    opts.gpu_method = 3
+    plan = ctypes.c_void_p(None)
+    assert mk(1, 3, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), opts) == 0
+    x = torch.zeros(64, dtype=torch.float32, device="cuda")
+    assert sp(64, x.data_ptr(), x.data_ptr(), x.data_ptr(), 0, None, None, None, plan) == 0
+    c = torch.zeros(64, dtype=torch.complex64, device="cuda")
+    fk = torch.zeros(16 ** 3, dtype=torch.complex64, device="cuda")
+    assert ex(c.data_ptr(), fk.data_ptr(), plan) == 2
+    assert de(plan) == 0
+    # execute before setpts is an error, not a crash
+    plan = ctypes.c_void_p(None)
+    assert mk(1, 3, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), None) == 0
+    assert ex(c.data_ptr(), fk.data_ptr(), plan) != 0
+    assert de(plan) == 0
+    # tolerance below machine precision is a swallowed warning
+    plan = ctypes.c_void_p(None)
+    assert mk(1, 2, nmodes, 1, 1, 1e-12, 0, ctypes.byref(plan), None) == 0
+    assert de(plan) == 0
+    # upsampfac <= 1 is error 7; Horner with sigma != 2 is error 8
+    # (contrib/spreadinterp.cpp:14-26)
+    opts = L.NufftOpts()
+    L._default_optsf(1, 2, opts)
+    opts.upsampfac = 0.9
+    plan = ctypes.c_void_p(None)
+    assert mk(1, 2, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), opts) == 7
+    de(plan)
+    opts.upsampfac = 1.25
+    opts.gpu_kerevalmeth = 1
+    plan = ctypes.c_void_p(None)
+    assert mk(1, 2, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), opts) == 8
+    de(plan)
+
+
+def test_upsampfac_125():
+    # sigma = 1.25 takes the reference's custom width/beta formulas
+    # (contrib/spreadinterp.cpp:40-61); results still meet the tolerance
+    for single, tol in ((True, 1e-4), (False, 1e-8)):
+        rng = np.random.default_rng(9)
+        modes = (30, 26)
+        dt = np.float32 if single else np.float64
+        pts = NC.points(rng, 2, 2000, dtype=dt)
+        c = NC.strengths(rng, 2000)
+        out, info = NC.run_gpu(1, modes, pts, c, tol, single, upsampfac=1.25)
+        idx = np.arange(int(np.prod(modes)))
+        d = NC.direct(1, modes, [p.astype(np.float64) for p in pts], c[0], 1, idx)
+        err = np.linalg.norm(out.ravel() - d) / np.linalg.norm(d)
+        assert err < 5 * max(tol, 2e-5 if single else 0), (err, info)
+        assert info["nf1"] < 2 * 30
