@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -30,6 +31,7 @@ template <typename T> struct Plan {
   cufinufft_opts opts;
   SpreaderParams sp{};
   int method = 0;  // method run: 1 (NU-point driven) or 2 (subproblem); 0 = invalid
+  int variant = 0; // kernel family: 0 warp-cooperative, 1 one thread per point
   int sort = 1;
   int bs[3] = {1, 1, 1}, nb[3] = {1, 1, 1};
   int nbins = 1;
@@ -220,6 +222,7 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
                          double tol, int maxbatchsize, const cufinufft_opts* opts) {
   p->type = type;
   p->dim = dim;
+  if (const char* v = std::getenv("CUFINUFFT_KERNEL_VARIANT")) p->variant = std::atoi(v) == 1 ? 1 : 0;
   if (opts) p->opts = *opts;
   else default_opts(type, dim, &p->opts);
   int ier = setup_spreader(tol, p->opts.upsampfac, p->opts.gpu_kerevalmeth, is_single<T>(), &p->sp);
@@ -425,6 +428,7 @@ static SpreadArgs<T> spread_args(Plan<T>* p) {
   a.kc.horner = p->horner;
   a.g.Nf = grid_cells(p);
   a.M = p->M;
+  a.variant = p->variant;
   return a;
 }
 

@@ -76,6 +76,7 @@ template <typename T> struct SpreadArgs {
   const cplx_t<T>* fw_in;   // type 2 input grid
   int ntr;
   int M;
+  int variant;              // 0: warp-cooperative kernels, 1: one thread per point
 };
 
 // Cells of one subproblem tile: the bin plus the ns-1 cells its points

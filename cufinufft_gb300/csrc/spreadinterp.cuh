@@ -281,6 +281,287 @@ k_interp_sm(SpreadArgs<T> a) {
 }
 
 // ---------------------------------------------------------------------------
+// Warp-cooperative variants.  A warp works on PPW = 32 / L points at a time;
+// the L >= ns lanes of a point cover its x taps, so every warp-wide memory
+// instruction touches PPW contiguous runs of ns cells (one row of each
+// point) instead of 32 scattered cells.  Lane j evaluates the x, y and z
+// kernel values of tap j; the y/z values of a row are broadcast with one
+// shuffle.  Interpolation reduces the L per-tap partial sums of a point with
+// a butterfly at the end.
+template <int NS> constexpr int lanes_per_point() {
+  return NS <= 2 ? 2 : (NS <= 4 ? 4 : (NS <= 8 ? 8 : 16));
+}
+
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_interp_gm_wc(SpreadArgs<T> a) {
+  using C = cplx_t<T>;
+  constexpr int HD = horner_degree<T>(NS);
+  constexpr int L = lanes_per_point<NS>();
+  constexpr int PPW = 32 / L;
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  const int lane = threadIdx.x & 31, g = lane / L, j = lane % L;
+  const bool tap = j < NS;
+  const int jj = tap ? j : 0;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
+  for (long long base = wid * PPW; base < a.M; base += nw * PPW) {
+    const long long pl = base + g;
+    const bool valid = pl < a.M;
+    const int p = valid ? (int)pl : a.M - 1;
+    const int xj = wrap_idx(a.pts.i0[0][p] + jj, nf0);
+    const T kx = kernel_tap<T, NS, HD>(a.pts.d[0][p], jj, a.kc);
+    T ky = T(1), kz = T(1);
+    int i2 = 0, i3 = 0;
+    if (DIM > 1) { i2 = a.pts.i0[1][p]; ky = kernel_tap<T, NS, HD>(a.pts.d[1][p], jj, a.kc); }
+    if (DIM > 2) { i3 = a.pts.i0[2][p]; kz = kernel_tap<T, NS, HD>(a.pts.d[2][p], jj, a.kc); }
+    const int dst = a.pts.idx[p];
+    for (int t = 0; t < a.ntr; ++t) {
+      const C* gt = a.fw_in + (size_t)t * a.g.Nf + xj;
+      T ar = T(0), ai = T(0);
+#pragma unroll 1
+      for (int dz = 0; dz < NZ; ++dz) {
+        const T kzv = DIM > 2 ? __shfl_sync(0xffffffffu, kz, g * L + dz) : T(1);
+        const int iz = DIM > 2 ? wrap_idx(i3 + dz, nf2) : 0;
+#pragma unroll
+        for (int dy = 0; dy < NY; ++dy) {
+          const T kyv = DIM > 1 ? __shfl_sync(0xffffffffu, ky, g * L + dy) : T(1);
+          const int iy = DIM > 1 ? wrap_idx(i2 + dy, nf1) : 0;
+          if (tap) {
+            const C v = __ldg(gt + ((size_t)iz * nf1 + iy) * nf0);
+            const T w = kyv * kzv;
+            ar = fma_rn(v.x, w, ar);
+            ai = fma_rn(v.y, w, ai);
+          }
+        }
+      }
+      ar *= kx;
+      ai *= kx;
+#pragma unroll
+      for (int off = L / 2; off > 0; off >>= 1) {
+        ar += __shfl_xor_sync(0xffffffffu, ar, off);
+        ai += __shfl_xor_sync(0xffffffffu, ai, off);
+      }
+      if (j == 0 && valid) {
+        C o;
+        o.x = ar;
+        o.y = ai;
+        a.c_out[(size_t)t * a.M + dst] = o;
+      }
+    }
+  }
+}
+
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_spread_gm_wc(SpreadArgs<T> a) {
+  using C = cplx_t<T>;
+  constexpr int HD = horner_degree<T>(NS);
+  constexpr int L = lanes_per_point<NS>();
+  constexpr int PPW = 32 / L;
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  const int lane = threadIdx.x & 31, g = lane / L, j = lane % L;
+  const bool tap = j < NS;
+  const int jj = tap ? j : 0;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
+  for (long long base = wid * PPW; base < a.M; base += nw * PPW) {
+    const long long pl = base + g;
+    const bool valid = pl < a.M;
+    const int p = valid ? (int)pl : a.M - 1;
+    const int xj = wrap_idx(a.pts.i0[0][p] + jj, nf0);
+    const T kx = kernel_tap<T, NS, HD>(a.pts.d[0][p], jj, a.kc);
+    T ky = T(1), kz = T(1);
+    int i2 = 0, i3 = 0;
+    if (DIM > 1) { i2 = a.pts.i0[1][p]; ky = kernel_tap<T, NS, HD>(a.pts.d[1][p], jj, a.kc); }
+    if (DIM > 2) { i3 = a.pts.i0[2][p]; kz = kernel_tap<T, NS, HD>(a.pts.d[2][p], jj, a.kc); }
+    const int src = a.pts.idx[p];
+    for (int t = 0; t < a.ntr; ++t) {
+      const C v = a.c_in[(size_t)t * a.M + src];
+      const T vr = v.x * kx, vi = v.y * kx;
+      C* gt = a.fw + (size_t)t * a.g.Nf + xj;
+#pragma unroll 1
+      for (int dz = 0; dz < NZ; ++dz) {
+        const T kzv = DIM > 2 ? __shfl_sync(0xffffffffu, kz, g * L + dz) : T(1);
+        const int iz = DIM > 2 ? wrap_idx(i3 + dz, nf2) : 0;
+#pragma unroll
+        for (int dy = 0; dy < NY; ++dy) {
+          const T kyv = DIM > 1 ? __shfl_sync(0xffffffffu, ky, g * L + dy) : T(1);
+          const int iy = DIM > 1 ? wrap_idx(i2 + dy, nf1) : 0;
+          const T w = kyv * kzv;
+          if (tap && valid) red_add(gt + ((size_t)iz * nf1 + iy) * nf0, vr * w, vi * w);
+        }
+      }
+    }
+  }
+}
+
+// Subproblem header shared by the shared-memory kernels.
+struct SubTile {
+  int p0, np, ox, oy, oz, TX, TY, TZ, ntile;
+};
+
+template <int DIM, int NS>
+__device__ __forceinline__ SubTile sub_tile(const BinTables& bt, int sub) {
+  SubTile s;
+  const int b = bt.sub_to_bin[sub];
+  const int js = sub - bt.sub_start[b];
+  s.p0 = bt.start[b] + js * bt.maxsub;
+  s.np = min(bt.maxsub, bt.count[b] - js * bt.maxsub);
+  const int bx = b % bt.nb[0];
+  const int by = (b / bt.nb[0]) % bt.nb[1];
+  const int bz = b / (bt.nb[0] * bt.nb[1]);
+  s.ox = bx * bt.bs[0];
+  s.oy = by * bt.bs[1];
+  s.oz = bz * bt.bs[2];
+  s.TX = bt.bs[0] + NS - 1;
+  s.TY = DIM > 1 ? bt.bs[1] + NS - 1 : 1;
+  s.TZ = DIM > 2 ? bt.bs[2] + NS - 1 : 1;
+  s.ntile = s.TX * s.TY * s.TZ;
+  return s;
+}
+
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_spread_sm_wc(SpreadArgs<T> a) {
+  using C = cplx_t<T>;
+  constexpr int HD = horner_degree<T>(NS);
+  constexpr int L = lanes_per_point<NS>();
+  constexpr int PPW = 32 / L;
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tile = reinterpret_cast<C*>(smem_raw);
+  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  const int t = blockIdx.y;
+  for (int i = threadIdx.x; i < st.ntile; i += blockDim.x) {
+    tile[i].x = T(0);
+    tile[i].y = T(0);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane / L, j = lane % L;
+  const bool tap = j < NS;
+  const int jj = tap ? j : 0;
+  const int warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  const C* cin = a.c_in + (size_t)t * a.M;
+  for (int base = warp * PPW; base < st.np; base += nwb * PPW) {
+    const int pl = base + g;
+    const bool valid = pl < st.np;
+    const int p = st.p0 + (valid ? pl : st.np - 1);
+    const int lx = a.pts.i0[0][p] - st.ox;
+    const T kx = kernel_tap<T, NS, HD>(a.pts.d[0][p], jj, a.kc);
+    T ky = T(1), kz = T(1);
+    int ly = 0, lz = 0;
+    if (DIM > 1) { ly = a.pts.i0[1][p] - st.oy; ky = kernel_tap<T, NS, HD>(a.pts.d[1][p], jj, a.kc); }
+    if (DIM > 2) { lz = a.pts.i0[2][p] - st.oz; kz = kernel_tap<T, NS, HD>(a.pts.d[2][p], jj, a.kc); }
+    const C v = cin[a.pts.idx[p]];
+    const T vr = v.x * kx, vi = v.y * kx;
+    C* row0 = tile + (lz * st.TY + ly) * st.TX + lx + jj;
+#pragma unroll 1
+    for (int dz = 0; dz < NZ; ++dz) {
+      const T kzv = DIM > 2 ? __shfl_sync(0xffffffffu, kz, g * L + dz) : T(1);
+#pragma unroll
+      for (int dy = 0; dy < NY; ++dy) {
+        const T kyv = DIM > 1 ? __shfl_sync(0xffffffffu, ky, g * L + dy) : T(1);
+        const T w = kyv * kzv;
+        if (tap && valid) smem_add(row0 + (dz * st.TY + dy) * st.TX, vr * w, vi * w);
+      }
+    }
+  }
+  __syncthreads();
+  C* gbase = a.fw + (size_t)t * a.g.Nf;
+  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
+  for (int i = threadIdx.x; i < st.ntile; i += blockDim.x) {
+    const C v = tile[i];
+    if (v.x == T(0) && v.y == T(0)) continue;
+    const int ix = i % st.TX;
+    const int iy = (i / st.TX) % st.TY;
+    const int iz = i / (st.TX * st.TY);
+    int gx = st.ox + ix, gy = st.oy + iy, gz = st.oz + iz;
+    while (gx >= nf0) gx -= nf0;
+    while (gy >= nf1) gy -= nf1;
+    while (gz >= nf2) gz -= nf2;
+    red_add(gbase + ((size_t)gz * nf1 + gy) * nf0 + gx, v.x, v.y);
+  }
+}
+
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_interp_sm_wc(SpreadArgs<T> a) {
+  using C = cplx_t<T>;
+  constexpr int HD = horner_degree<T>(NS);
+  constexpr int L = lanes_per_point<NS>();
+  constexpr int PPW = 32 / L;
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* tile = reinterpret_cast<C*>(smem_raw);
+  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  const int t = blockIdx.y;
+  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
+  const C* gbase = a.fw_in + (size_t)t * a.g.Nf;
+  for (int i = threadIdx.x; i < st.ntile; i += blockDim.x) {
+    const int ix = i % st.TX;
+    const int iy = (i / st.TX) % st.TY;
+    const int iz = i / (st.TX * st.TY);
+    int gx = st.ox + ix, gy = st.oy + iy, gz = st.oz + iz;
+    while (gx >= nf0) gx -= nf0;
+    while (gy >= nf1) gy -= nf1;
+    while (gz >= nf2) gz -= nf2;
+    tile[i] = __ldg(gbase + ((size_t)gz * nf1 + gy) * nf0 + gx);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane / L, j = lane % L;
+  const bool tap = j < NS;
+  const int jj = tap ? j : 0;
+  const int warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  for (int base = warp * PPW; base < st.np; base += nwb * PPW) {
+    const int pl = base + g;
+    const bool valid = pl < st.np;
+    const int p = st.p0 + (valid ? pl : st.np - 1);
+    const int lx = a.pts.i0[0][p] - st.ox;
+    const T kx = kernel_tap<T, NS, HD>(a.pts.d[0][p], jj, a.kc);
+    T ky = T(1), kz = T(1);
+    int ly = 0, lz = 0;
+    if (DIM > 1) { ly = a.pts.i0[1][p] - st.oy; ky = kernel_tap<T, NS, HD>(a.pts.d[1][p], jj, a.kc); }
+    if (DIM > 2) { lz = a.pts.i0[2][p] - st.oz; kz = kernel_tap<T, NS, HD>(a.pts.d[2][p], jj, a.kc); }
+    const C* row0 = tile + (lz * st.TY + ly) * st.TX + lx + jj;
+    T ar = T(0), ai = T(0);
+#pragma unroll 1
+    for (int dz = 0; dz < NZ; ++dz) {
+      const T kzv = DIM > 2 ? __shfl_sync(0xffffffffu, kz, g * L + dz) : T(1);
+#pragma unroll
+      for (int dy = 0; dy < NY; ++dy) {
+        const T kyv = DIM > 1 ? __shfl_sync(0xffffffffu, ky, g * L + dy) : T(1);
+        if (tap) {
+          const C v = row0[(dz * st.TY + dy) * st.TX];
+          const T w = kyv * kzv;
+          ar = fma_rn(v.x, w, ar);
+          ai = fma_rn(v.y, w, ai);
+        }
+      }
+    }
+    ar *= kx;
+    ai *= kx;
+#pragma unroll
+    for (int off = L / 2; off > 0; off >>= 1) {
+      ar += __shfl_xor_sync(0xffffffffu, ar, off);
+      ai += __shfl_xor_sync(0xffffffffu, ai, off);
+    }
+    if (j == 0 && valid) {
+      C o;
+      o.x = ar;
+      o.y = ai;
+      a.c_out[(size_t)t * a.M + a.pts.idx[p]] = o;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Launchers, instantiated per (T, DIM) in si_*.cu.
 
 inline int grid_for(long long n, int threads) {
@@ -305,15 +586,24 @@ cudaError_t prepare_smem(K kernel, size_t bytes) {
 template <typename T, int DIM, int NS>
 cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
   if (a.M == 0) return cudaSuccess;
+  const bool wc = a.variant == 0;
   if (method == 1) {
-    k_spread_gm<T, DIM, NS><<<grid_for(a.M, kSpreadThreads), kSpreadThreads, 0, s>>>(a);
+    if (wc) {
+      constexpr int PPW = 32 / lanes_per_point<NS>();
+      k_spread_gm_wc<T, DIM, NS><<<grid_for(((long long)a.M + PPW - 1) / PPW * 32, kSpreadThreads),
+                                   kSpreadThreads, 0, s>>>(a);
+    } else {
+      k_spread_gm<T, DIM, NS><<<grid_for(a.M, kSpreadThreads), kSpreadThreads, 0, s>>>(a);
+    }
   } else {
     if (a.bins.nsub == 0) return cudaSuccess;
     size_t sm = tile_bytes<T, DIM>(NS, a.bins);
-    cudaError_t e = prepare_smem(k_spread_sm<T, DIM, NS>, sm);
+    cudaError_t e = wc ? prepare_smem(k_spread_sm_wc<T, DIM, NS>, sm)
+                       : prepare_smem(k_spread_sm<T, DIM, NS>, sm);
     if (e != cudaSuccess) return e;
     dim3 grid(a.bins.nsub, a.ntr);
-    k_spread_sm<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
+    if (wc) k_spread_sm_wc<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
+    else k_spread_sm<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
   }
   return cudaGetLastError();
 }
@@ -321,15 +611,24 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
 template <typename T, int DIM, int NS>
 cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
   if (a.M == 0) return cudaSuccess;
+  const bool wc = a.variant == 0;
   if (method == 1) {
-    k_interp_gm<T, DIM, NS><<<grid_for(a.M, kSpreadThreads), kSpreadThreads, 0, s>>>(a);
+    if (wc) {
+      constexpr int PPW = 32 / lanes_per_point<NS>();
+      k_interp_gm_wc<T, DIM, NS><<<grid_for(((long long)a.M + PPW - 1) / PPW * 32, kSpreadThreads),
+                                   kSpreadThreads, 0, s>>>(a);
+    } else {
+      k_interp_gm<T, DIM, NS><<<grid_for(a.M, kSpreadThreads), kSpreadThreads, 0, s>>>(a);
+    }
   } else {
     if (a.bins.nsub == 0) return cudaSuccess;
     size_t sm = tile_bytes<T, DIM>(NS, a.bins);
-    cudaError_t e = prepare_smem(k_interp_sm<T, DIM, NS>, sm);
+    cudaError_t e = wc ? prepare_smem(k_interp_sm_wc<T, DIM, NS>, sm)
+                       : prepare_smem(k_interp_sm<T, DIM, NS>, sm);
     if (e != cudaSuccess) return e;
     dim3 grid(a.bins.nsub, a.ntr);
-    k_interp_sm<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
+    if (wc) k_interp_sm_wc<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
+    else k_interp_sm<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
   }
   return cudaGetLastError();
 }

@@ -23,6 +23,11 @@ TYPE1_METHODS = {1: [(1, 1), (1, 0), (2, 1)], 2: [(1, 1), (1, 0), (2, 1), (3, 1)
 TYPE2_METHODS = {1: [(1, 1), (1, 0)], 2: [(1, 1), (1, 0), (2, 1)], 3: [(1, 1), (1, 0), (2, 1)]}
 
 
+def info_beta(tol, single):
+    from oracle import oracle as O
+    return O.setup_spreader(tol, single)[2]
+
+
 def _bounds(single, tol, kerevalmeth):
     same = (2e-5 if single else 1e-10)
     if kerevalmeth == 1:
@@ -32,10 +37,10 @@ def _bounds(single, tol, kerevalmeth):
 
 
 def _case(ntype, dim, method, sort, single, kerevalmeth, tol, M=1500, ntr=1, maxbatch=1, seed=0,
-          lo=-3 * np.pi, hi=3 * np.pi, **extra):
+          lo=-3 * np.pi, hi=3 * np.pi, edges=False, **extra):
     rng = np.random.default_rng(seed + 17 * dim + 5 * ntype + 3 * method)
     modes = MODES[dim]
-    pts = NC.points(rng, dim, M, lo, hi, dtype=np.float32 if single else np.float64)
+    pts = NC.points(rng, dim, M, lo, hi, dtype=np.float32 if single else np.float64, edges=edges)
     if ntype == 1:
         data = NC.strengths(rng, M, ntr)
     else:
@@ -48,6 +53,12 @@ def _case(ntype, dim, method, sort, single, kerevalmeth, tol, M=1500, ntr=1, max
     ref = NC.oracle_nufft(ntype, modes, [p.astype(np.float64) for p in pts],
                           data.astype(np.complex128), tol, single, ntr=ntr, gpu_method=method)
     same, dbound = _bounds(single, tol, kerevalmeth)
+    if edges:
+        # a point exactly on a fold boundary (x = -pi, pi, -3pi) sits where
+        # the kernel is cut off at |x| = ns/2; position roundings ~1e-16 of
+        # the two implementations pick the tap on either side of the cut,
+        # which moves that point's contribution by exp(-beta) of the peak
+        same = max(same, 2.0 * np.exp(-info_beta(tol, single)))
     err_same = float(np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel()))
     assert err_same < same, (err_same, info)
     iflag = 1 if ntype == 1 else -1
@@ -126,6 +137,15 @@ def test_clustered_points_many_subproblems():
         for ntype in (1, 2):
             _case(ntype, 2, 2, 1, single, 0, 1e-5 if single else 1e-9, M=20000, lo=0.1, hi=0.12,
                   gpu_maxsubprobsize=256)
+
+
+@pytest.mark.parametrize("single", [True, False], ids=["f32", "f64"])
+@pytest.mark.parametrize("ntype", [1, 2])
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_fold_boundary_points(single, ntype, dim):
+    # points exactly at -3pi, -pi, 0, pi, -2pi and just inside 3pi
+    tol = 1e-3 if single else 1e-6
+    _case(ntype, dim, 2 if (ntype == 1 or dim > 1) else 1, 1, single, 0, tol, edges=True, seed=21)
 
 
 def test_points_in_principal_range_only():
