@@ -346,10 +346,44 @@ def run_reference(args, w: Workload, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args, w: Workload, rank, world, local_rank):
+def _make_plan(w: Workload, dev, stream, opts):
     import torch
 
     from cufinufft_gb300 import cufinufft
+    plan = cufinufft(w.ntype, w.modes[::-1], n_trans=w.ntransf, eps=w.tol, dtype=w.rdt,
+                     isign=1 if w.ntype == 1 else -1, **opts)
+    plan.set_stream(stream)
+    return plan
+
+
+def _io_tensors(w: Workload, data_dev, M, dev):
+    import torch
+    ctorch = torch.complex64 if w.single else torch.complex128
+    if w.ntype == 1:
+        out = torch.zeros((w.ntransf,) + w.modes[::-1], dtype=ctorch, device=dev)
+        return data_dev, out, (data_dev, out)
+    out = torch.zeros((w.ntransf, M), dtype=ctorch, device=dev)
+    return data_dev, out, (out, data_dev)
+
+
+def _time_device(plan, args_ce, steps, stream, flush):
+    """Device time (ms) of `steps` executes, L2 flushed before each (outside
+    the events)."""
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for i in range(steps):
+            flush.fill_(float(i))
+            ev[i][0].record(stream)
+            plan.execute(*args_ce)
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev)
+
+
+def run_ours(args, w: Workload, rank, world, local_rank):
+    import torch
     dev = torch.device("cuda", local_rank)
     torch.cuda.set_device(dev)
     dist = None
@@ -358,27 +392,18 @@ def run_ours(args, w: Workload, rank, world, local_rank):
     pts = w.points()
     M = pts[0].size
     data = w.data()
-    opts = {}
-    if args.method:
-        opts["gpu_method"] = args.method
+    # tuned form: the library chooses the method (gpu_method 0) unless given
+    opts = {"gpu_method": args.method}
     if args.kerevalmeth is not None:
         opts["gpu_kerevalmeth"] = args.kerevalmeth
     stream = torch.cuda.Stream(device=dev)
-    plan = cufinufft(w.ntype, w.modes[::-1], n_trans=w.ntransf, eps=w.tol, dtype=w.rdt,
-                     isign=1 if w.ntype == 1 else -1, **opts)
-    plan.set_stream(stream)
+    plan = _make_plan(w, dev, stream, opts)
     pts_dev = [torch.from_numpy(p).to(dev) for p in pts]
     data_dev = torch.from_numpy(data).to(dev)
-    ctorch = torch.complex64 if w.single else torch.complex128
-    if w.ntype == 1:
-        inp, out = data_dev, torch.zeros((w.ntransf,) + w.modes[::-1], dtype=ctorch, device=dev)
-        c_arg, fk_arg = inp, out
-    else:
-        inp, out = data_dev, torch.zeros((w.ntransf, M), dtype=ctorch, device=dev)
-        c_arg, fk_arg = out, inp
+    inp, out, args_ce = _io_tensors(w, data_dev, M, dev)
     with torch.cuda.stream(stream):
         plan.set_pts(*pts_dev[::-1])  # the Python interface takes C-ordered axes
-        plan.execute(c_arg, fk_arg)
+        plan.execute(*args_ce)
     torch.cuda.synchronize()
     info = plan.info()
     out_first = out.cpu().numpy()
@@ -391,66 +416,106 @@ def run_ours(args, w: Workload, rank, world, local_rank):
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             flush.fill_(1.0)
-            plan.execute(c_arg, fk_arg)
+            plan.execute(*args_ce)
     torch.cuda.synchronize()
 
     # ---- timed: device-resident inputs
     plan.set_timing(True)
     plan.stage_times(reset=True)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
     clocks = ClockSampler(local_rank)
     clocks.start()
     barrier()
     torch.cuda.synchronize()
     t_start = time.time()
-    with torch.cuda.stream(stream):
-        for i in range(args.steps):
-            flush.fill_(float(i))
-            ev[i][0].record(stream)
-            plan.execute(c_arg, fk_arg)
-            ev[i][1].record(stream)
-    torch.cuda.synchronize()
+    dev_ms = _time_device(plan, args_ce, args.steps, stream, flush)
     t_end = time.time()
     barrier()
     clk = clocks.stop(t_start, t_end)
-    dev_ms = sum(a.elapsed_time(b) for a, b in ev)
     stages = plan.stage_times(reset=True)
     plan.set_timing(False)
 
-    # ---- e2e: host buffers, copies inside each step
-    inp_host = torch.from_numpy(data.copy()).pin_memory()
-    out_host = torch.empty(out.shape, dtype=ctorch).pin_memory()
-    inp_stage = torch.empty_like(inp)
-    c2, f2 = (inp_stage, out) if w.ntype == 1 else (out, inp_stage)
-    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            inp_stage.copy_(inp_host, non_blocking=True)
-            plan.execute(c2, f2)
-            out_host.copy_(out, non_blocking=True)
-    torch.cuda.synchronize()
-    barrier()
-    with torch.cuda.stream(stream):
-        for i in range(args.steps):
-            flush.fill_(float(i))
-            ev2[i][0].record(stream)
-            inp_stage.copy_(inp_host, non_blocking=True)
-            plan.execute(c2, f2)
-            out_host.copy_(out, non_blocking=True)
-            ev2[i][1].record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    e2e_ms = sum(a.elapsed_time(b) for a, b in ev2)
-    scale = float(np.abs(out_first).max())
-    if not np.allclose(out_host.numpy(), out_first, rtol=0, atol=1e-4 * scale):
-        raise RuntimeError("e2e output differs from the device-resident run")
+    # ---- plain form: the reference's default options, same inputs
+    plain_ms = None
+    if not args.no_plain:
+        plain = _make_plan(w, dev, stream, {})
+        with torch.cuda.stream(stream):
+            plain.set_pts(*pts_dev[::-1])
+            for _ in range(args.warmup):
+                plain.execute(*args_ce)
+        torch.cuda.synchronize()
+        plain_steps = max(3, min(args.steps, 200))
+        plain_ms = _time_device(plain, args_ce, plain_steps, stream, flush) / plain_steps
+        plain_info = plain.info()
+        del plain
 
-    times = torch.tensor([dev_ms, e2e_ms], dtype=torch.float64, device=dev)
+    # ---- e2e: host buffers through the public call; every step copies its
+    # input from pinned host memory and its output back.  Two plans on two
+    # streams alternate so one step's copies overlap the other's compute.
+    inp_host = torch.from_numpy(data.copy()).pin_memory()
+    out_host = torch.empty((2,) + tuple(out.shape), dtype=out.dtype).pin_memory()
+    streams = [stream, torch.cuda.Stream(device=dev)]
+    plans = [plan, _make_plan(w, dev, streams[1], opts)]
+    with torch.cuda.stream(streams[1]):
+        plans[1].set_pts(*pts_dev[::-1])
+    stage_in = [torch.empty_like(inp) for _ in range(2)]
+    stage_out = [torch.empty_like(out) for _ in range(2)]
+
+    def ce(k):
+        return (stage_in[k], stage_out[k]) if w.ntype == 1 else (stage_out[k], stage_in[k])
+
+    def e2e_serial(steps):
+        # per step: [events] H2D -> execute -> D2H [events]; L2 flushed
+        # between steps outside the events
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        st = streams[0]
+        with torch.cuda.stream(st):
+            for i in range(steps):
+                flush.fill_(float(i))
+                ev[i][0].record(st)
+                stage_in[0].copy_(inp_host, non_blocking=True)
+                plans[0].execute(*ce(0))
+                out_host[0].copy_(stage_out[0], non_blocking=True)
+                ev[i][1].record(st)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev)
+
+    def e2e_pipelined(steps):
+        # a continuous stream of transforms: two plans alternate, so one
+        # step's copies overlap the other's compute (no flush in between)
+        done = [torch.cuda.Event() for _ in range(2)]
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(streams[0])
+        streams[1].wait_event(t0)
+        for i in range(steps):
+            k = i % 2
+            st = streams[k]
+            with torch.cuda.stream(st):
+                stage_in[k].copy_(inp_host, non_blocking=True)
+                plans[k].execute(*ce(k))
+                out_host[k].copy_(stage_out[k], non_blocking=True)
+                done[k].record(st)
+        streams[0].wait_event(done[1])
+        t1.record(streams[0])
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1)
+
+    e2e_serial(min(args.warmup, 20))
+    e2e_pipelined(max(2, min(args.warmup, 20)))
+    barrier()
+    e2e_ms = e2e_serial(args.steps)
+    e2e_pipe_ms = e2e_pipelined(args.steps)
+    barrier()
+    scale = float(np.abs(out_first).max())
+    for k in range(2):
+        if not np.allclose(out_host[k].numpy(), out_first, rtol=0, atol=1e-4 * scale):
+            raise RuntimeError("e2e output differs from the device-resident run")
+
+    times = torch.tensor([dev_ms, e2e_ms, e2e_pipe_ms], dtype=torch.float64, device=dev)
     if dist is not None:
         dist.all_reduce(times, op=dist.ReduceOp.MAX)
-    dev_ms, e2e_ms = float(times[0]), float(times[1])
+    dev_ms, e2e_ms, e2e_pipe_ms = float(times[0]), float(times[1]), float(times[2])
     if rank != 0:
         return
 
@@ -493,11 +558,26 @@ def run_ours(args, w: Workload, rank, world, local_rank):
         "config": {"workload": w.desc, "name": w.name, "global_batch": world, "seq_len": None,
                    "parallelism": f"replicas x{world}",
                    "l2": "flushed between steps (256 MB write, outside the timed events)",
+                   "form": "tuned (gpu_method chosen by the library)" if args.method == 0
+                   else f"gpu_method {args.method}",
                    "method": info["method"], "ns": info["ns"], "nf": nf[:w.dim],
                    "kerevalmeth": info["kerevalmeth"]},
         "rel_l2_err": err, "rel_l2_points": nacc, "tol": w.tol,
+        "plain": None if plain_ms is None else {
+            "value": units / (plain_ms / 1e3), "ms_per_step": plain_ms,
+            "method": plain_info["method"],
+            "note": "reference default options (type 1: gpu_method 2, type 2: gpu_method 1)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(data.nbytes),
-                "d2h_bytes_per_step": int(out.numel() * out.element_size())},
+                "d2h_bytes_per_step": int(out.numel() * out.element_size()),
+                "ms_per_step": e2e_ms / args.steps,
+                "note": "public Python/C-ABI execute with the input copied from pinned host "
+                        "memory and the output copied back inside each step's events; L2 "
+                        "flushed between steps",
+                "pipelined": {"value": world * units * args.steps / (e2e_pipe_ms / 1e3),
+                              "ms_per_step": e2e_pipe_ms / args.steps,
+                              "note": "same calls as a continuous stream: two plans on two "
+                                      "streams alternate so one step's copies overlap the "
+                                      "other's compute; no L2 flush between steps"}},
         "gpu_launches": 2 * int(math.ceil(w.ntransf / max(info["maxbatchsize"], 1))) * args.steps,
         "roofline": roof,
         "cpu_baseline": cpu,
@@ -514,10 +594,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="radial2d")
-    ap.add_argument("--method", type=int, default=0, help="gpu_method override (0 = default)")
+    ap.add_argument("--method", type=int, default=0,
+                    help="gpu_method for the timed plan (0 = chosen by the library)")
     ap.add_argument("--kerevalmeth", type=int, default=None)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the direct-sum check")
+    ap.add_argument("--no-plain", action="store_true", help="skip the default-options plan")
     args = ap.parse_args()
     if args.impl == "ours":
         args.warmup = max(args.warmup, 3)

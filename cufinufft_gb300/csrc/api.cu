@@ -31,7 +31,8 @@ template <typename T> struct Plan {
   cufinufft_opts opts;
   SpreaderParams sp{};
   int method = 0;  // method run: 1 (NU-point driven) or 2 (subproblem); 0 = invalid
-  int variant = 0; // kernel family: 0 warp-cooperative, 1 one thread per point
+  int variant = 0; // kernel family: 0 default, 1 one thread per point, 2 warp-cooperative
+  bool auto_method = false;  // gpu_method 0: chosen by the library
   int sort = 1;
   int bs[3] = {1, 1, 1}, nb[3] = {1, 1, 1};
   int nbins = 1;
@@ -44,7 +45,8 @@ template <typename T> struct Plan {
   int rem = 0;
   C* fw = nullptr;
   T* fac[3] = {nullptr, nullptr, nullptr};
-  T* horner = nullptr;
+  std::vector<T> horner;  // fitted kernel polynomials (kerevalmeth 1), [k][j]
+  T* horner_d = nullptr;  // device copy of the same
   // sorted points and bin tables
   int* idx = nullptr;
   int* i0[3] = {nullptr, nullptr, nullptr};
@@ -183,8 +185,9 @@ template <typename T> static void release(Plan<T>* p) {
     cudaFree(p->fac[k]);
     p->fac[k] = nullptr;
   }
-  cudaFree(p->horner);
-  p->horner = nullptr;
+  p->horner.clear();
+  cudaFree(p->horner_d);
+  p->horner_d = nullptr;
   free_points(p);
   cudaFree(p->count);
   cudaFree(p->start);
@@ -222,7 +225,10 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
                          double tol, int maxbatchsize, const cufinufft_opts* opts) {
   p->type = type;
   p->dim = dim;
-  if (const char* v = std::getenv("CUFINUFFT_KERNEL_VARIANT")) p->variant = std::atoi(v) == 1 ? 1 : 0;
+  if (const char* v = std::getenv("CUFINUFFT_KERNEL_VARIANT")) {
+    const int k = std::atoi(v);
+    p->variant = (k == 1 || k == 2) ? k : 0;
+  }
   if (opts) p->opts = *opts;
   else default_opts(type, dim, &p->opts);
   int ier = setup_spreader(tol, p->opts.upsampfac, p->opts.gpu_kerevalmeth, is_single<T>(), &p->sp);
@@ -232,7 +238,17 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
 
   // method actually run (src/2d/spread2d_wrapper.cu:99-164,
   // src/3d/spread3d_wrapper.cu:101-160, src/*/interp*_wrapper.cu):
-  const int m = p->opts.gpu_method;
+  int m = p->opts.gpu_method;
+  if (m == 0) {
+    // extension: gpu_method 0 lets the library choose (the reference rejects
+    // 0).  Measured on GB300: spreading is fastest NU-point driven into the
+    // grid (vector reductions in L2); interpolation from shared-memory tiles
+    // in 2D/3D.
+    m = (type == 1 || dim == 1) ? 1 : 2;
+    p->opts.gpu_method = m;
+    p->opts.gpu_sort = 1;
+    p->auto_method = true;
+  }
   p->sort = p->opts.gpu_sort;
   int bins_from_obin = 0;
   if (type == 1) {
@@ -301,14 +317,13 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   fseries_nodes(p->sp, &nodes);
   CFG_CUDA(launch_fseries<T>(nodes, dim, p->nf, p->N, p->fac[0], p->fac[1], p->fac[2], p->stream));
 
-  std::vector<T> hh;
   if (p->opts.gpu_kerevalmeth == 1) {
     const int deg = horner_degree<T>(p->sp.ns);
     std::vector<double> cd = horner_fit(p->sp, deg);
-    hh.assign(cd.begin(), cd.end());
-    CFG_CUDA(cudaMalloc(&p->horner, sizeof(T) * hh.size()));
-    CFG_CUDA(cudaMemcpyAsync(p->horner, hh.data(), sizeof(T) * hh.size(), cudaMemcpyHostToDevice,
-                             p->stream));
+    p->horner.assign(cd.begin(), cd.end());
+    CFG_CUDA(cudaMalloc(&p->horner_d, sizeof(T) * p->horner.size()));
+    CFG_CUDA(cudaMemcpyAsync(p->horner_d, p->horner.data(), sizeof(T) * p->horner.size(),
+                             cudaMemcpyHostToDevice, p->stream));
   }
   CFG_CUDA(cudaStreamSynchronize(p->stream));
   p->planned = true;
@@ -425,7 +440,10 @@ static SpreadArgs<T> spread_args(Plan<T>* p) {
   a.bins.maxsub = p->opts.gpu_maxsubprobsize;
   a.kc.beta = (T)p->sp.beta;
   a.kc.c = (T)p->sp.c;
-  a.kc.horner = p->horner;
+  a.kc.horner = p->horner.empty() ? 0 : 1;
+  a.kc.coef_g = p->horner_d;
+  for (size_t k = 0; k < p->horner.size() && k < (size_t)(kMaxHornerRows * kMaxNS); ++k)
+    a.kc.coef[k] = p->horner[k];
   a.g.Nf = grid_cells(p);
   a.M = p->M;
   a.variant = p->variant;

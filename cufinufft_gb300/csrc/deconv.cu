@@ -93,8 +93,35 @@ k_deconvolve(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, const c
   }
 }
 
-// One block row per fine-grid row (w2, w3); threads over w1.  Rows outside
-// the mode band and cells between the positive and negative x-modes are 0.
+// One block row per fine-grid row (w2, w3); each thread writes two adjacent
+// cells (one 16-byte store in FP32).  Rows outside the mode band and cells
+// between the positive and negative x-modes are 0.
+template <typename T>
+__device__ __forceinline__ cplx_t<T> amp_cell(int w1, int nf0, int N0, const cplx_t<T>* src,
+                                              const T* __restrict__ fac0, T f23) {
+  cplx_t<T> o;
+  const int k1 = w1 <= (N0 - 1) / 2 ? w1 : (w1 >= nf0 - N0 / 2 ? w1 - nf0 : nf0);
+  if (k1 == nf0) {
+    o.x = T(0);
+    o.y = T(0);
+  } else {
+    const int i1 = k1 + N0 / 2;
+    const T f = fac0[i1] * f23;
+    const cplx_t<T> v = src[i1];
+    o.x = v.x * f;
+    o.y = v.y * f;
+  }
+  return o;
+}
+
+__device__ __forceinline__ void store_pair(float2* dst, float2 a, float2 b) {
+  *reinterpret_cast<float4*>(dst) = make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void store_pair(double2* dst, double2 a, double2 b) {
+  dst[0] = a;
+  dst[1] = b;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_amplify(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, cplx_t<T>* __restrict__ fw,
@@ -104,11 +131,11 @@ k_amplify(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, cplx_t<T>*
   const long long Nf = (long long)nf0 * nf1 * nf2;
   const long long Nm = (long long)N0 * N1 * N2;
   const int nrows = nf1 * nf2;
+  const int npairs = nf0 / 2;  // nf0 is even
   for (int r = blockIdx.x; r < nrows * ntr; r += gridDim.x) {
     const int t = r / nrows;
     const int rr = r - t * nrows;
     const int w2 = rr % nf1, w3 = rr / nf1;
-    // mode index along y/z, or -1 when the row carries no modes
     int i2 = 0, i3 = 0;
     bool live = true;
     if (dim > 1) {
@@ -123,32 +150,20 @@ k_amplify(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, cplx_t<T>*
     }
     C* dst = fw + (size_t)t * Nf + ((size_t)w3 * nf1 + w2) * nf0;
     if (!live) {
-      for (int w1 = threadIdx.x; w1 < nf0; w1 += blockDim.x) {
-        C z;
-        z.x = T(0);
-        z.y = T(0);
-        dst[w1] = z;
-      }
+      C z;
+      z.x = T(0);
+      z.y = T(0);
+      for (int q = threadIdx.x; q < npairs; q += blockDim.x) store_pair(dst + 2 * q, z, z);
       continue;
     }
     T f23 = T(1);
     if (dim > 1) f23 = fac1[i2];
     if (dim > 2) f23 *= fac2[i3];
     const C* src = fk + (size_t)t * Nm + ((size_t)i3 * N1 + i2) * N0;
-    for (int w1 = threadIdx.x; w1 < nf0; w1 += blockDim.x) {
-      const int k1 = w1 <= (N0 - 1) / 2 ? w1 : (w1 >= nf0 - N0 / 2 ? w1 - nf0 : nf0);
-      C o;
-      if (k1 == nf0) {
-        o.x = T(0);
-        o.y = T(0);
-      } else {
-        const int i1 = k1 + N0 / 2;
-        const T f = fac0[i1] * f23;
-        const C v = src[i1];
-        o.x = v.x * f;
-        o.y = v.y * f;
-      }
-      dst[w1] = o;
+    for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
+      const C a = amp_cell<T>(2 * q, nf0, N0, src, fac0, f23);
+      const C b = amp_cell<T>(2 * q + 1, nf0, N0, src, fac0, f23);
+      store_pair(dst + 2 * q, a, b);
     }
   }
 }

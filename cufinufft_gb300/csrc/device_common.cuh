@@ -65,32 +65,39 @@ __device__ __forceinline__ void place_coord(T x, const AxisMap<T>& a, int& i0, T
 }
 
 // ---- ES kernel values -----------------------------------------------------
-__device__ __forceinline__ float es_exp(float z, float beta) { return expf(beta * sqrtf(1.0f - z)); }
-__device__ __forceinline__ double es_exp(double z, double beta) { return exp(beta * sqrt(1.0 - z)); }
+// phi = exp(beta*sqrt(1 - z)) for z = c x^2 < 1, else 0; evaluated without a
+// branch (the square root of a clamped argument, then a select).
+__device__ __forceinline__ float es_value(float z, float beta) {
+  const float e = expf(beta * sqrtf(fmaxf(1.0f - z, 0.0f)));
+  return z < 1.0f ? e : 0.0f;
+}
+__device__ __forceinline__ double es_value(double z, double beta) {
+  const double e = exp(beta * sqrt(fmax(1.0 - z, 0.0)));
+  return z < 1.0 ? e : 0.0;
+}
 
 // ker[j] = phi(d - ns/2 + j), j = 0..NS-1, phi(x) = exp(beta*sqrt(1-c x^2))
 // for |x| < ns/2 and 0 outside (src/cuspreadinterp.h:6-40).  With
-// horner != nullptr the values come from the plan's fitted piecewise
-// polynomials in z = 2d - 1 (coefficient k of tap j at horner[k*NS + j],
+// kc.horner set the values come from the plan's fitted piecewise
+// polynomials in z = 2d - 1 (coefficient k of tap j at coef[k*NS + j],
 // highest degree first, HDEG+1 rows).
 template <typename T, int NS, int HDEG>
 __device__ __forceinline__ void kernel_row(T d, const KernelCoeffs<T>& kc, T* ker) {
-  if (kc.horner != nullptr) {
+  if (kc.horner) {
     const T z = T(2) * d - T(1);
 #pragma unroll
-    for (int j = 0; j < NS; ++j) ker[j] = __ldg(kc.horner + j);
+    for (int j = 0; j < NS; ++j) ker[j] = kc.coef[j];
 #pragma unroll
     for (int k = 1; k <= HDEG; ++k) {
 #pragma unroll
-      for (int j = 0; j < NS; ++j) ker[j] = fma_rn(ker[j], z, __ldg(kc.horner + k * NS + j));
+      for (int j = 0; j < NS; ++j) ker[j] = fma_rn(ker[j], z, kc.coef[k * NS + j]);
     }
   } else {
     const T x0 = d - T(0.5) * T(NS);
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
-      T x = x0 + T(j);
-      T z = kc.c * x * x;
-      ker[j] = (z < T(1)) ? es_exp(z, kc.beta) : T(0);
+      const T x = x0 + T(j);
+      ker[j] = es_value(kc.c * x * x, kc.beta);
     }
   }
 }
@@ -99,16 +106,15 @@ __device__ __forceinline__ void kernel_row(T d, const KernelCoeffs<T>& kc, T* ke
 // the outermost axis of 3D loops, which are not unrolled).
 template <typename T, int NS, int HDEG>
 __device__ __forceinline__ T kernel_tap(T d, int j, const KernelCoeffs<T>& kc) {
-  if (kc.horner != nullptr) {
+  if (kc.horner) {
     const T z = T(2) * d - T(1);
-    T v = __ldg(kc.horner + j);
+    T v = __ldg(kc.coef_g + j);
 #pragma unroll
-    for (int k = 1; k <= HDEG; ++k) v = fma_rn(v, z, __ldg(kc.horner + k * NS + j));
+    for (int k = 1; k <= HDEG; ++k) v = fma_rn(v, z, __ldg(kc.coef_g + k * NS + j));
     return v;
   }
   const T x = d - T(0.5) * T(NS) + T(j);
-  const T z = kc.c * x * x;
-  return (z < T(1)) ? es_exp(z, kc.beta) : T(0);
+  return es_value(kc.c * x * x, kc.beta);
 }
 
 // ---- atomics ---------------------------------------------------------------

@@ -31,11 +31,18 @@ template <typename T> struct AxisMap {
   int nf, half_int;
 };
 
-// Kernel-evaluation constants: phi(x) = exp(beta*sqrt(1 - c x^2)), or the
-// fitted polynomials when horner != nullptr.
+constexpr int kMaxHornerRows = kMaxNS + 4;  // degree <= ns + 3
+
+// Kernel-evaluation constants: phi(x) = exp(beta*sqrt(1 - c x^2)), or, when
+// horner != 0, the fitted polynomials: coef[k*ns + j] is the coefficient of
+// z^(deg-k) for tap j.  The coefficients travel inside the kernel's
+// parameter block, so the unrolled evaluation reads them straight from the
+// constant bank.
 template <typename T> struct KernelCoeffs {
   T beta, c;
-  const T* horner;
+  int horner;
+  const T* coef_g;                   // device copy, read by kernel_tap (runtime tap index)
+  T coef[kMaxHornerRows * kMaxNS];
 };
 
 // Bin-sorted points in plan memory (written by setpts).
@@ -76,7 +83,7 @@ template <typename T> struct SpreadArgs {
   const cplx_t<T>* fw_in;   // type 2 input grid
   int ntr;
   int M;
-  int variant;              // 0: warp-cooperative kernels, 1: one thread per point
+  int variant;              // kernel family: 0 default, 1 one thread per point, 2 warp-cooperative
 };
 
 // Cells of one subproblem tile: the bin plus the ns-1 cells its points

@@ -27,6 +27,85 @@ namespace cfg {
 
 constexpr int kSpreadThreads = 256;
 
+// Subproblem header shared by the shared-memory kernels.
+struct SubTile {
+  int p0, np, ox, oy, oz, TX, TY, TZ, ntile;
+};
+
+template <int DIM, int NS>
+__device__ __forceinline__ SubTile sub_tile(const BinTables& bt, int sub) {
+  SubTile s;
+  const int b = bt.sub_to_bin[sub];
+  const int js = sub - bt.sub_start[b];
+  s.p0 = bt.start[b] + js * bt.maxsub;
+  s.np = min(bt.maxsub, bt.count[b] - js * bt.maxsub);
+  const int bx = b % bt.nb[0];
+  const int by = (b / bt.nb[0]) % bt.nb[1];
+  const int bz = b / (bt.nb[0] * bt.nb[1]);
+  s.ox = bx * bt.bs[0];
+  s.oy = by * bt.bs[1];
+  s.oz = bz * bt.bs[2];
+  s.TX = bt.bs[0] + NS - 1;
+  s.TY = DIM > 1 ? bt.bs[1] + NS - 1 : 1;
+  s.TZ = DIM > 2 ? bt.bs[2] + NS - 1 : 1;
+  s.ntile = s.TX * s.TY * s.TZ;
+  return s;
+}
+
+// Copy the subproblem's padded tile from the fine grid (periodic wrap) into
+// shared memory: one warp per tile row, lanes along x.
+template <typename T>
+__device__ __forceinline__ void tile_load(cplx_t<T>* tile, const cplx_t<T>* grid, const SubTile& st,
+                                          const GridGeom& g) {
+  const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
+  const int rows = st.TY * st.TZ;
+  for (int r = threadIdx.x >> 5; r < rows; r += nwb) {
+    const int iy = r % st.TY, iz = r / st.TY;
+    int gy = st.oy + iy, gz = st.oz + iz;
+    while (gy >= g.nf[1]) gy -= g.nf[1];
+    while (gz >= g.nf[2]) gz -= g.nf[2];
+    const cplx_t<T>* src = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
+    cplx_t<T>* dst = tile + r * st.TX;
+    for (int ix = lane; ix < st.TX; ix += 32) {
+      int gx = st.ox + ix;
+      while (gx >= g.nf[0]) gx -= g.nf[0];
+      dst[ix] = __ldg(src + gx);
+    }
+  }
+}
+
+// Add the tile back into the fine grid with vector reductions, skipping the
+// cells no point touched.
+template <typename T>
+__device__ __forceinline__ void tile_flush(const cplx_t<T>* tile, cplx_t<T>* grid, const SubTile& st,
+                                           const GridGeom& g) {
+  const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
+  const int rows = st.TY * st.TZ;
+  for (int r = threadIdx.x >> 5; r < rows; r += nwb) {
+    const int iy = r % st.TY, iz = r / st.TY;
+    int gy = st.oy + iy, gz = st.oz + iz;
+    while (gy >= g.nf[1]) gy -= g.nf[1];
+    while (gz >= g.nf[2]) gz -= g.nf[2];
+    cplx_t<T>* dst = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
+    const cplx_t<T>* src = tile + r * st.TX;
+    for (int ix = lane; ix < st.TX; ix += 32) {
+      const cplx_t<T> v = src[ix];
+      if (v.x == T(0) && v.y == T(0)) continue;
+      int gx = st.ox + ix;
+      while (gx >= g.nf[0]) gx -= g.nf[0];
+      red_add(dst + gx, v.x, v.y);
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void tile_zero(cplx_t<T>* tile, int ntile) {
+  for (int i = threadIdx.x; i < ntile; i += blockDim.x) {
+    tile[i].x = T(0);
+    tile[i].y = T(0);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Method 1: NU-point driven spread.
 template <typename T, int DIM, int NS>
@@ -83,69 +162,38 @@ k_spread_sm(SpreadArgs<T> a) {
   constexpr int NZ = DIM > 2 ? NS : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tile = reinterpret_cast<C*>(smem_raw);
-
-  const BinTables& bt = a.bins;
-  const int sub = blockIdx.x, t = blockIdx.y;
-  const int b = bt.sub_to_bin[sub];
-  const int js = sub - bt.sub_start[b];
-  const int p0 = bt.start[b] + js * bt.maxsub;
-  const int np = min(bt.maxsub, bt.count[b] - js * bt.maxsub);
-  const int bx = b % bt.nb[0];
-  const int by = (b / bt.nb[0]) % bt.nb[1];
-  const int bz = b / (bt.nb[0] * bt.nb[1]);
-  const int ox = bx * bt.bs[0], oy = by * bt.bs[1], oz = bz * bt.bs[2];
-  const int TX = bt.bs[0] + NS - 1;
-  const int TY = DIM > 1 ? bt.bs[1] + NS - 1 : 1;
-  const int TZ = DIM > 2 ? bt.bs[2] + NS - 1 : 1;
-  const int ntile = TX * TY * TZ;
-
-  for (int i = threadIdx.x; i < ntile; i += blockDim.x) {
-    tile[i].x = T(0);
-    tile[i].y = T(0);
-  }
+  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  const int t = blockIdx.y;
+  tile_zero<T>(tile, st.ntile);
   __syncthreads();
-
   const C* cin = a.c_in + (size_t)t * a.M;
-  for (int p = p0 + threadIdx.x; p < p0 + np; p += blockDim.x) {
+  for (int p = st.p0 + threadIdx.x; p < st.p0 + st.np; p += blockDim.x) {
     T k1[NS], k2[NS];
-    const int lx = a.pts.i0[0][p] - ox;
+    const int lx = a.pts.i0[0][p] - st.ox;
     kernel_row<T, NS, HD>(a.pts.d[0][p], a.kc, k1);
     int ly = 0, lz = 0;
-    if (DIM > 1) { ly = a.pts.i0[1][p] - oy; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
+    if (DIM > 1) { ly = a.pts.i0[1][p] - st.oy; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
     T d3 = T(0);
-    if (DIM > 2) { lz = a.pts.i0[2][p] - oz; d3 = a.pts.d[2][p]; }
+    if (DIM > 2) { lz = a.pts.i0[2][p] - st.oz; d3 = a.pts.d[2][p]; }
     const C v = cin[a.pts.idx[p]];
 #pragma unroll 1
     for (int dz = 0; dz < NZ; ++dz) {
       const T kz = DIM > 2 ? kernel_tap<T, NS, HD>(d3, dz, a.kc) : T(1);
+      C* plane = tile + ((lz + dz) * st.TY + ly) * st.TX + lx;
 #pragma unroll
       for (int dy = 0; dy < NY; ++dy) {
         T kyz = T(1);
         if (DIM > 1) kyz = k2[dy];
         if (DIM > 2) kyz *= kz;
         const T vr = v.x * kyz, vi = v.y * kyz;
-        C* row = tile + ((lz + dz) * TY + (ly + dy)) * TX + lx;
+        C* row = plane + dy * st.TX;
 #pragma unroll
         for (int dx = 0; dx < NS; ++dx) smem_add(row + dx, vr * k1[dx], vi * k1[dx]);
       }
     }
   }
   __syncthreads();
-
-  C* base = a.fw + (size_t)t * a.g.Nf;
-  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
-  for (int i = threadIdx.x; i < ntile; i += blockDim.x) {
-    const C v = tile[i];
-    if (v.x == T(0) && v.y == T(0)) continue;
-    const int ix = i % TX;
-    const int iy = (i / TX) % TY;
-    const int iz = i / (TX * TY);
-    int gx = ox + ix, gy = oy + iy, gz = oz + iz;
-    while (gx >= nf0) gx -= nf0;
-    while (gy >= nf1) gy -= nf1;
-    while (gz >= nf2) gz -= nf2;
-    red_add(base + ((size_t)gz * nf1 + gy) * nf0 + gx, v.x, v.y);
-  }
+  tile_flush<T>(tile, a.fw + (size_t)t * a.g.Nf, st, a.g);
 }
 
 // ---------------------------------------------------------------------------
@@ -214,51 +262,26 @@ k_interp_sm(SpreadArgs<T> a) {
   constexpr int NZ = DIM > 2 ? NS : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tile = reinterpret_cast<C*>(smem_raw);
-
-  const BinTables& bt = a.bins;
-  const int sub = blockIdx.x, t = blockIdx.y;
-  const int b = bt.sub_to_bin[sub];
-  const int js = sub - bt.sub_start[b];
-  const int p0 = bt.start[b] + js * bt.maxsub;
-  const int np = min(bt.maxsub, bt.count[b] - js * bt.maxsub);
-  const int bx = b % bt.nb[0];
-  const int by = (b / bt.nb[0]) % bt.nb[1];
-  const int bz = b / (bt.nb[0] * bt.nb[1]);
-  const int ox = bx * bt.bs[0], oy = by * bt.bs[1], oz = bz * bt.bs[2];
-  const int TX = bt.bs[0] + NS - 1;
-  const int TY = DIM > 1 ? bt.bs[1] + NS - 1 : 1;
-  const int TZ = DIM > 2 ? bt.bs[2] + NS - 1 : 1;
-  const int ntile = TX * TY * TZ;
-  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
-
-  const C* base = a.fw_in + (size_t)t * a.g.Nf;
-  for (int i = threadIdx.x; i < ntile; i += blockDim.x) {
-    const int ix = i % TX;
-    const int iy = (i / TX) % TY;
-    const int iz = i / (TX * TY);
-    int gx = ox + ix, gy = oy + iy, gz = oz + iz;
-    while (gx >= nf0) gx -= nf0;
-    while (gy >= nf1) gy -= nf1;
-    while (gz >= nf2) gz -= nf2;
-    tile[i] = __ldg(base + ((size_t)gz * nf1 + gy) * nf0 + gx);
-  }
+  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  const int t = blockIdx.y;
+  tile_load<T>(tile, a.fw_in + (size_t)t * a.g.Nf, st, a.g);
   __syncthreads();
-
-  for (int p = p0 + threadIdx.x; p < p0 + np; p += blockDim.x) {
+  for (int p = st.p0 + threadIdx.x; p < st.p0 + st.np; p += blockDim.x) {
     T k1[NS], k2[NS];
-    const int lx = a.pts.i0[0][p] - ox;
+    const int lx = a.pts.i0[0][p] - st.ox;
     kernel_row<T, NS, HD>(a.pts.d[0][p], a.kc, k1);
     int ly = 0, lz = 0;
-    if (DIM > 1) { ly = a.pts.i0[1][p] - oy; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
+    if (DIM > 1) { ly = a.pts.i0[1][p] - st.oy; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
     T d3 = T(0);
-    if (DIM > 2) { lz = a.pts.i0[2][p] - oz; d3 = a.pts.d[2][p]; }
+    if (DIM > 2) { lz = a.pts.i0[2][p] - st.oz; d3 = a.pts.d[2][p]; }
     T ar = T(0), ai = T(0);
 #pragma unroll 1
     for (int dz = 0; dz < NZ; ++dz) {
       const T kz = DIM > 2 ? kernel_tap<T, NS, HD>(d3, dz, a.kc) : T(1);
+      const C* plane = tile + ((lz + dz) * st.TY + ly) * st.TX + lx;
 #pragma unroll
       for (int dy = 0; dy < NY; ++dy) {
-        const C* row = tile + ((lz + dz) * TY + (ly + dy)) * TX + lx;
+        const C* row = plane + dy * st.TX;
         T rr = T(0), ri = T(0);
 #pragma unroll
         for (int dx = 0; dx < NS; ++dx) {
@@ -400,31 +423,6 @@ k_spread_gm_wc(SpreadArgs<T> a) {
   }
 }
 
-// Subproblem header shared by the shared-memory kernels.
-struct SubTile {
-  int p0, np, ox, oy, oz, TX, TY, TZ, ntile;
-};
-
-template <int DIM, int NS>
-__device__ __forceinline__ SubTile sub_tile(const BinTables& bt, int sub) {
-  SubTile s;
-  const int b = bt.sub_to_bin[sub];
-  const int js = sub - bt.sub_start[b];
-  s.p0 = bt.start[b] + js * bt.maxsub;
-  s.np = min(bt.maxsub, bt.count[b] - js * bt.maxsub);
-  const int bx = b % bt.nb[0];
-  const int by = (b / bt.nb[0]) % bt.nb[1];
-  const int bz = b / (bt.nb[0] * bt.nb[1]);
-  s.ox = bx * bt.bs[0];
-  s.oy = by * bt.bs[1];
-  s.oz = bz * bt.bs[2];
-  s.TX = bt.bs[0] + NS - 1;
-  s.TY = DIM > 1 ? bt.bs[1] + NS - 1 : 1;
-  s.TZ = DIM > 2 ? bt.bs[2] + NS - 1 : 1;
-  s.ntile = s.TX * s.TY * s.TZ;
-  return s;
-}
-
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
 k_spread_sm_wc(SpreadArgs<T> a) {
@@ -438,10 +436,7 @@ k_spread_sm_wc(SpreadArgs<T> a) {
   C* tile = reinterpret_cast<C*>(smem_raw);
   const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
   const int t = blockIdx.y;
-  for (int i = threadIdx.x; i < st.ntile; i += blockDim.x) {
-    tile[i].x = T(0);
-    tile[i].y = T(0);
-  }
+  tile_zero<T>(tile, st.ntile);
   __syncthreads();
   const int lane = threadIdx.x & 31, g = lane / L, j = lane % L;
   const bool tap = j < NS;
@@ -473,20 +468,7 @@ k_spread_sm_wc(SpreadArgs<T> a) {
     }
   }
   __syncthreads();
-  C* gbase = a.fw + (size_t)t * a.g.Nf;
-  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
-  for (int i = threadIdx.x; i < st.ntile; i += blockDim.x) {
-    const C v = tile[i];
-    if (v.x == T(0) && v.y == T(0)) continue;
-    const int ix = i % st.TX;
-    const int iy = (i / st.TX) % st.TY;
-    const int iz = i / (st.TX * st.TY);
-    int gx = st.ox + ix, gy = st.oy + iy, gz = st.oz + iz;
-    while (gx >= nf0) gx -= nf0;
-    while (gy >= nf1) gy -= nf1;
-    while (gz >= nf2) gz -= nf2;
-    red_add(gbase + ((size_t)gz * nf1 + gy) * nf0 + gx, v.x, v.y);
-  }
+  tile_flush<T>(tile, a.fw + (size_t)t * a.g.Nf, st, a.g);
 }
 
 template <typename T, int DIM, int NS>
@@ -502,18 +484,7 @@ k_interp_sm_wc(SpreadArgs<T> a) {
   C* tile = reinterpret_cast<C*>(smem_raw);
   const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
   const int t = blockIdx.y;
-  const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
-  const C* gbase = a.fw_in + (size_t)t * a.g.Nf;
-  for (int i = threadIdx.x; i < st.ntile; i += blockDim.x) {
-    const int ix = i % st.TX;
-    const int iy = (i / st.TX) % st.TY;
-    const int iz = i / (st.TX * st.TY);
-    int gx = st.ox + ix, gy = st.oy + iy, gz = st.oz + iz;
-    while (gx >= nf0) gx -= nf0;
-    while (gy >= nf1) gy -= nf1;
-    while (gz >= nf2) gz -= nf2;
-    tile[i] = __ldg(gbase + ((size_t)gz * nf1 + gy) * nf0 + gx);
-  }
+  tile_load<T>(tile, a.fw_in + (size_t)t * a.g.Nf, st, a.g);
   __syncthreads();
   const int lane = threadIdx.x & 31, g = lane / L, j = lane % L;
   const bool tap = j < NS;
@@ -583,10 +554,14 @@ cudaError_t prepare_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// Kernel family per stage (SpreadArgs::variant 0 = the measured default):
+// spreading is warp-cooperative for both methods; interpolation is
+// warp-cooperative for method 1 and one-thread-per-point for method 2.
+// variant 1 forces one thread per point, 2 forces warp-cooperative.
 template <typename T, int DIM, int NS>
 cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
   if (a.M == 0) return cudaSuccess;
-  const bool wc = a.variant == 0;
+  const bool wc = a.variant != 1;
   if (method == 1) {
     if (wc) {
       constexpr int PPW = 32 / lanes_per_point<NS>();
@@ -611,7 +586,7 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
 template <typename T, int DIM, int NS>
 cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
   if (a.M == 0) return cudaSuccess;
-  const bool wc = a.variant == 0;
+  const bool wc = method == 1 ? a.variant != 1 : a.variant == 2;
   if (method == 1) {
     if (wc) {
       constexpr int PPW = 32 / lanes_per_point<NS>();

@@ -151,3 +151,14 @@ def test_fold_boundary_points(single, ntype, dim):
 def test_points_in_principal_range_only():
     _case(1, 2, 2, 1, True, 0, 1e-6, lo=-np.pi, hi=np.pi)
     _case(2, 3, 1, 1, False, 0, 1e-10, lo=-np.pi, hi=np.pi)
+
+
+@pytest.mark.parametrize("single", [True, False], ids=["f32", "f64"])
+@pytest.mark.parametrize("ntype", [1, 2])
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_library_chosen_method(single, ntype, dim):
+    # gpu_method 0 (an extension: the reference rejects it) lets the library
+    # pick the method; results are the same algorithm's
+    tol = 1e-5 if single else 1e-9
+    info = _case(ntype, dim, 0, 1, single, 0, tol, seed=31)
+    assert info["method"] in (1, 2)
