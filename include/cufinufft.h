@@ -119,6 +119,24 @@ int cufinufftf_set_timing(cufinufftf_plan plan, int on);
 int cufinufft_stage_times(cufinufft_plan plan, double* ms, long long* batches, int reset);
 int cufinufftf_stage_times(cufinufftf_plan plan, double* ms, long long* batches, int reset);
 
+/* Allocation-free spreading; it has no counterpart in the reference.  For
+ * callers that cannot allocate device memory at the point of use (code inside
+ * a framework that owns all device memory, real-time loops, memory-budgeted
+ * services): spreads M points (x, y in [-3pi, 3pi), strengths c, all device
+ * arrays) onto the caller's nf1 x nf2 fine grid fw (x fastest), which this
+ * call zeroes first, with the ES kernel of FP32 tolerance tol -- the type-1
+ * spreading stage of a plan with that fine grid (bin sort, 32x32 bins,
+ * shared-memory subproblems) -- on `stream`, without allocating: its sort
+ * scratch is a fixed device array of about 3.2 MB that every GPU loading
+ * the library holds.  Limits: M <= 131072 and at most 4096 bins (fine grids
+ * up to 2048 x 2048); larger requests return CUFINUFFT_ERR_ARG.  All calls on
+ * a device share that scratch: calls whose GPU work overlaps race and must be
+ * serialised by the caller.  The first call on each device looks up the
+ * scratch address, so make it before any stream capture. */
+int cufinufftf_spread2d_noalloc(int M, const float* x, const float* y, const cuFloatComplex* c,
+                                int nf1, int nf2, float tol, cuFloatComplex* fw,
+                                cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
