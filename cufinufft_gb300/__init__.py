@@ -7,12 +7,13 @@ reference's ``cufinufft`` Python package.  The library is loaded on first use
 of ``cufinufft`` (so ``cufinufft_gb300.build`` can run before it exists).
 """
 
-__all__ = ["cufinufft"]
+__all__ = ["cufinufft", "cufinufft_batch"]
 
 
 def __getattr__(name):
-    if name == "cufinufft":
-        from cufinufft_gb300._interface import cufinufft as cls
-        globals()["cufinufft"] = cls
+    if name in ("cufinufft", "cufinufft_batch"):
+        from cufinufft_gb300 import _interface
+        cls = getattr(_interface, name)
+        globals()[name] = cls
         return cls
     raise AttributeError(name)

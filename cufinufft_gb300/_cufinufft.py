@@ -148,3 +148,64 @@ _stage_times.restype = c_int
 _stage_timesf = lib.cufinufftf_stage_times
 _stage_timesf.argtypes = [c_void_p, c_double_p, ctypes.POINTER(ctypes.c_longlong), c_int]
 _stage_timesf.restype = c_int
+_batch_make = lib.cufinufft_batch_make
+_batch_make.argtypes = [c_int, ctypes.POINTER(c_void_p), ctypes.POINTER(c_void_p)]
+_batch_make.restype = c_int
+_batch_makef = lib.cufinufftf_batch_make
+_batch_makef.argtypes = [c_int, ctypes.POINTER(c_void_p), ctypes.POINTER(c_void_p)]
+_batch_makef.restype = c_int
+_batch_execute = lib.cufinufft_batch_execute
+_batch_execute.argtypes = [c_void_p, ctypes.POINTER(c_void_p), ctypes.POINTER(c_void_p)]
+_batch_execute.restype = c_int
+_batch_executef = lib.cufinufftf_batch_execute
+_batch_executef.argtypes = [c_void_p, ctypes.POINTER(c_void_p), ctypes.POINTER(c_void_p)]
+_batch_executef.restype = c_int
+_batch_destroy = lib.cufinufft_batch_destroy
+_batch_destroy.argtypes = [c_void_p]
+_batch_destroy.restype = c_int
+_batch_destroyf = lib.cufinufftf_batch_destroy
+_batch_destroyf.argtypes = [c_void_p]
+_batch_destroyf.restype = c_int
+
+
+class TuneEntry(ctypes.Structure):
+    """Mirror of cufinufft_tune_entry (autotuning record)."""
+    _fields_ = [("method", c_int), ("binsizex", c_int), ("binsizey", c_int), ("binsizez", c_int),
+                ("maxsubprobsize", c_int), ("ms", c_float)]
+
+
+for _name in ("cufinufft_set_layout", "cufinufftf_set_layout"):
+    getattr(lib, _name).argtypes = [c_void_p, c_int, c_int, c_int, c_int, c_int]
+    getattr(lib, _name).restype = c_int
+for _name in ("cufinufft_autotune", "cufinufftf_autotune"):
+    getattr(lib, _name).argtypes = [c_void_p, ctypes.POINTER(TuneEntry), c_int, c_int_p]
+    getattr(lib, _name).restype = c_int
+_set_layout = lib.cufinufft_set_layout
+_set_layoutf = lib.cufinufftf_set_layout
+_autotune = lib.cufinufft_autotune
+_autotunef = lib.cufinufftf_autotune
+
+# Learned layout selector: plan features, layout classes and the MLP kernels.
+MLP_FEATURES, MLP_HIDDEN, MLP_CLASSES = 14, 32, 9
+MLP_PARAMS = (MLP_HIDDEN * MLP_FEATURES + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN
+              + MLP_CLASSES * MLP_HIDDEN + MLP_CLASSES)
+for _name in ("cufinufft_features", "cufinufftf_features"):
+    getattr(lib, _name).argtypes = [c_void_p, c_void_p]
+    getattr(lib, _name).restype = c_int
+for _name in ("cufinufft_set_layout_class", "cufinufftf_set_layout_class"):
+    getattr(lib, _name).argtypes = [c_void_p, c_int]
+    getattr(lib, _name).restype = c_int
+_features = lib.cufinufft_features
+_featuresf = lib.cufinufftf_features
+_set_layout_class = lib.cufinufft_set_layout_class
+_set_layout_classf = lib.cufinufftf_set_layout_class
+mlp_forward = lib.cufinufft_mlp_forward
+mlp_forward.argtypes = [c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p]
+mlp_forward.restype = c_int
+mlp_grad = lib.cufinufft_mlp_grad
+mlp_grad.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_void_p, c_void_p,
+                     c_void_p, c_void_p]
+mlp_grad.restype = c_int
+mlp_adam = lib.cufinufft_mlp_adam
+mlp_adam.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_void_p]
+mlp_adam.restype = c_int

@@ -207,6 +207,48 @@ class cufinufft:
             raise RuntimeError('Error reading stage times.')
         return {"spreadinterp": ms[0], "fft": ms[1], "deconv": ms[2], "batches": nb.value}
 
+    def set_layout(self, method, binsize, maxsubprobsize=1024) -> None:
+        """Re-sort the points for another method (1 or 2), bin size (tuple in
+        the library's x, y, z order) and subproblem cap; results unchanged."""
+        from cufinufft_gb300._cufinufft import _set_layout, _set_layoutf
+        fn = _set_layout if self.dtype == np.float64 else _set_layoutf
+        b = tuple(binsize) + (1,) * (3 - len(binsize))
+        ier = fn(self.plan, int(method), int(b[0]), int(b[1]), int(b[2]), int(maxsubprobsize))
+        if ier != 0:
+            raise RuntimeError(f'Error setting layout ({ier}).')
+
+    def autotune(self) -> list:
+        """Time candidate layouts on this plan's points and keep the fastest.
+        Returns the chosen entry followed by every candidate tried."""
+        from cufinufft_gb300._cufinufft import TuneEntry, _autotune, _autotunef
+        fn = _autotune if self.dtype == np.float64 else _autotunef
+        buf = (TuneEntry * 64)()
+        n = ctypes.c_int(0)
+        ier = fn(self.plan, buf, 64, ctypes.byref(n))
+        if ier != 0:
+            raise RuntimeError(f'Error autotuning ({ier}).')
+        return [{f: getattr(buf[i], f) for f, _ in TuneEntry._fields_} for i in range(n.value)]
+
+    def features(self) -> np.ndarray:
+        """The layout-independent plan features the learned selector reads
+        (14 floats, computed from the points' occupancy of the fine grid)."""
+        from cufinufft_gb300._cufinufft import MLP_FEATURES, _features, _featuresf
+        fn = _features if self.dtype == np.float64 else _featuresf
+        f = np.zeros(MLP_FEATURES, dtype=np.float32)
+        ier = fn(self.plan, f.ctypes.data)
+        if ier != 0:
+            raise RuntimeError(f'Error computing features ({ier}).')
+        return f
+
+    def set_layout_class(self, cls: int) -> None:
+        """Re-sort the points into one of the nine layout classes (the
+        selector's and autotuner's candidates)."""
+        from cufinufft_gb300._cufinufft import _set_layout_class, _set_layout_classf
+        fn = _set_layout_class if self.dtype == np.float64 else _set_layout_classf
+        ier = fn(self.plan, int(cls))
+        if ier != 0:
+            raise RuntimeError(f'Error setting layout class ({ier}).')
+
     def info(self) -> dict:
         """Plan facts: fine grid, kernel width, method run, bins."""
         inf = PlanInfo()
@@ -222,3 +264,53 @@ class cufinufft:
             raise RuntimeError('Error destroying plan.')
         self.plan = None
         self.references = []
+
+
+class cufinufft_batch:
+    """Many plans of one type, dimension, dtype and tolerance-derived kernel
+    width executed together (an extension with no counterpart in the
+    reference).  ``plans`` are ``cufinufft`` objects whose points are set;
+    they must stay alive, with their points, as long as the batch.
+    ``execute(c_list, fk_list)`` takes one (c, fk) pair per plan, as that
+    plan's ``execute`` would, and runs all of them in one CUDA-graph replay."""
+
+    def __init__(self, plans):
+        from cufinufft_gb300._cufinufft import (_batch_destroy, _batch_destroyf, _batch_execute,
+                                                _batch_executef, _batch_make, _batch_makef)
+        self.batch = None
+        self.plans = list(plans)
+        if not self.plans:
+            raise ValueError("a batch needs at least one plan")
+        dt = self.plans[0].dtype
+        if any(p.dtype != dt for p in self.plans):
+            raise TypeError("all plans of a batch must share one dtype")
+        self.dtype = dt
+        self.complex_dtype = self.plans[0].complex_dtype
+        make = _batch_make if dt == np.float64 else _batch_makef
+        self._exec = _batch_execute if dt == np.float64 else _batch_executef
+        self._destroy = _batch_destroy if dt == np.float64 else _batch_destroyf
+        arr = (c_void_p * len(self.plans))(*[p.plan.value for p in self.plans])
+        self.batch = c_void_p(None)
+        ier = make(len(self.plans), arr, byref(self.batch))
+        if ier != 0:
+            self.batch = None
+            raise RuntimeError(f'Error creating batch ({ier}).')
+
+    def execute(self, c_list, fk_list):
+        n = len(self.plans)
+        if len(c_list) != n or len(fk_list) != n:
+            raise TypeError("execute expects one c and one fk per plan")
+        for c, fk in zip(c_list, fk_list):
+            if not (_np_dtype(c) == _np_dtype(fk) == self.complex_dtype):
+                raise TypeError("cufinufft batch execute expects {} arrays".format(self.complex_dtype))
+        cs = (c_void_p * n)(*[_ptr(c) for c in c_list])
+        fks = (c_void_p * n)(*[_ptr(f) for f in fk_list])
+        ier = self._exec(self.batch, cs, fks)
+        if ier != 0:
+            raise RuntimeError(f'Error executing batch ({ier}).')
+
+    def __del__(self):
+        if exiting or self.batch is None or not self.batch.value:
+            return
+        self._destroy(self.batch)
+        self.batch = None

@@ -16,101 +16,10 @@
 #include <new>
 #include <vector>
 
-#include "../../include/cufinufft.h"
-#include "kernels.h"
-#include "planner.h"
+#include "plan.h"
+#include "selector_weights.h"
 
 namespace cfg {
-
-template <typename T> struct Plan {
-  using C = cplx_t<T>;
-  int type = 0, dim = 0;
-  int N[3] = {1, 1, 1};
-  int nf[3] = {1, 1, 1};
-  int ntransf = 1, maxbatch = 1, iflag = 1;
-  cufinufft_opts opts;
-  SpreaderParams sp{};
-  int method = 0;  // method run: 1 (NU-point driven) or 2 (subproblem); 0 = invalid
-  int variant = 0; // kernel family: 0 default, 1 one thread per point, 2 warp-cooperative
-  bool auto_method = false;  // gpu_method 0: chosen by the library
-  int sort = 1;
-  int bs[3] = {1, 1, 1}, nb[3] = {1, 1, 1};
-  int nbins = 1;
-  int device = 0;
-  int M = 0, nsub = 0;
-  bool planned = false, pts_set = false;
-  cudaStream_t own = nullptr, stream = nullptr;
-  cufftHandle fft = 0, fft_rem = 0;
-  bool have_fft = false, have_fft_rem = false;
-  int rem = 0;
-  C* fw = nullptr;
-  T* fac[3] = {nullptr, nullptr, nullptr};
-  std::vector<T> horner;  // fitted kernel polynomials (kerevalmeth 1), [k][j]
-  T* horner_d = nullptr;  // device copy of the same
-  // sorted points and bin tables
-  int* idx = nullptr;
-  int* i0[3] = {nullptr, nullptr, nullptr};
-  T* d[3] = {nullptr, nullptr, nullptr};
-  int* rank = nullptr;
-  size_t capM = 0;
-  int* count = nullptr;
-  int* start = nullptr;
-  int* sub_start = nullptr;
-  int* scan_tmp = nullptr;
-  int* sub_to_bin = nullptr;
-  size_t cap_sub = 0;
-  int* h_total = nullptr;  // pinned readback of the subproblem count
-  // stage timing (extension): events recorded around each stage of execute
-  bool timing = false;
-  std::vector<cudaEvent_t> ev_pool;   // free events
-  std::vector<cudaEvent_t> ev_live;   // groups of 4 per batch, not yet read
-  double stage_ms[3] = {0, 0, 0};     // spread|interp, fft, deconv|amplify
-  long long stage_batches = 0;
-};
-
-// Restores the caller's current device on scope exit.
-struct DeviceGuard {
-  int prev = -1;
-  bool ok = false;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    ok = cudaSetDevice(dev) == cudaSuccess;
-  }
-  ~DeviceGuard() {
-    if (prev >= 0) cudaSetDevice(prev);
-  }
-};
-
-#define CFG_CUDA(call)                                             \
-  do {                                                             \
-    cudaError_t e_ = (call);                                       \
-    if (e_ != cudaSuccess) {                                       \
-      fprintf(stderr, "cufinufft: %s failed: %s\n", #call, cudaGetErrorString(e_)); \
-      return e_ == cudaErrorMemoryAllocation ? CUFINUFFT_ERR_ALLOC : CUFINUFFT_ERR_CUDA; \
-    }                                                              \
-  } while (0)
-
-#define CFG_CUFFT(call)                                            \
-  do {                                                             \
-    cufftResult r_ = (call);                                       \
-    if (r_ != CUFFT_SUCCESS) {                                     \
-      fprintf(stderr, "cufinufft: %s failed: cufftResult %d\n", #call, (int)r_); \
-      return r_ == CUFFT_ALLOC_FAILED ? CUFINUFFT_ERR_ALLOC : CUFINUFFT_ERR_CUFFT; \
-    }                                                              \
-  } while (0)
-
-template <typename T> constexpr bool is_single() { return sizeof(T) == 4; }
-
-template <typename T> cufftType fft_type();
-template <> cufftType fft_type<float>() { return CUFFT_C2C; }
-template <> cufftType fft_type<double>() { return CUFFT_Z2Z; }
-
-static cufftResult fft_exec(cufftHandle h, float2* data, int dir) {
-  return cufftExecC2C(h, (cufftComplex*)data, (cufftComplex*)data, dir);
-}
-static cufftResult fft_exec(cufftHandle h, double2* data, int dir) {
-  return cufftExecZ2Z(h, (cufftDoubleComplex*)data, (cufftDoubleComplex*)data, dir);
-}
 
 // Defaults, restating CUFINUFFT_DEFAULT_OPTS (src/cufinufft.cu:639-730).
 int default_opts(int type, int dim, cufinufft_opts* opts) {
@@ -186,6 +95,8 @@ template <typename T> static void release(Plan<T>* p) {
     p->fac[k] = nullptr;
   }
   p->horner.clear();
+  cudaFree(p->sel_buf);
+  p->sel_buf = nullptr;
   cudaFree(p->horner_d);
   p->horner_d = nullptr;
   free_points(p);
@@ -205,10 +116,6 @@ template <typename T> static void release(Plan<T>* p) {
   if (p->own) cudaStreamDestroy(p->own);
   p->own = p->stream = nullptr;
   p->planned = p->pts_set = false;
-}
-
-template <typename T> static long long grid_cells(const Plan<T>* p) {
-  return (long long)p->nf[0] * p->nf[1] * p->nf[2];
 }
 
 template <typename T>
@@ -346,19 +253,7 @@ static int ensure_points(Plan<T>* p, int M) {
 }
 
 template <typename T>
-static AxisMap<T> axis_map(int nf, int ns) {
-  AxisMap<T> a;
-  const double S = (double)nf / (2.0 * M_PI);
-  a.s_hi = (T)S;
-  a.s_lo = (T)(S - (double)a.s_hi);
-  a.o_lo = (T)(1.5 * nf);
-  a.o_mid = (T)(0.5 * nf);
-  a.o_hi = (T)(-0.5 * nf);
-  a.half_int = ns / 2;
-  a.half_frac = (ns % 2) ? T(0.5) : T(0);
-  a.nf = nf;
-  return a;
-}
+static int select_layout(Plan<T>* p);
 
 template <typename T>
 static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
@@ -415,57 +310,7 @@ static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
   }
   CFG_CUDA(cudaGetLastError());
   p->pts_set = true;
-  return 0;
-}
-
-template <typename T>
-static SpreadArgs<T> spread_args(Plan<T>* p) {
-  SpreadArgs<T> a;
-  std::memset(&a, 0, sizeof(a));
-  a.pts.idx = p->idx;
-  for (int k = 0; k < 3; ++k) {
-    a.pts.i0[k] = p->i0[k];
-    a.pts.d[k] = p->d[k];
-    a.bins.bs[k] = p->bs[k];
-    a.bins.nb[k] = p->nb[k];
-    a.g.nf[k] = p->nf[k];
-  }
-  a.pts.M = p->M;
-  a.bins.nbins = p->nbins;
-  a.bins.count = p->count;
-  a.bins.start = p->start;
-  a.bins.sub_start = p->sub_start;
-  a.bins.sub_to_bin = p->sub_to_bin;
-  a.bins.nsub = p->nsub;
-  a.bins.maxsub = p->opts.gpu_maxsubprobsize;
-  a.kc.beta = (T)p->sp.beta;
-  a.kc.c = (T)p->sp.c;
-  a.kc.horner = p->horner.empty() ? 0 : 1;
-  a.kc.coef_g = p->horner_d;
-  for (size_t k = 0; k < p->horner.size() && k < (size_t)(kMaxHornerRows * kMaxNS); ++k)
-    a.kc.coef[k] = p->horner[k];
-  a.g.Nf = grid_cells(p);
-  a.M = p->M;
-  a.variant = p->variant;
-  return a;
-}
-
-template <typename T>
-static cudaError_t run_spread(Plan<T>* p, const SpreadArgs<T>& a) {
-  switch (p->dim) {
-    case 1: return spread_dim<T, 1>(p->method, p->sp.ns, a, p->stream);
-    case 2: return spread_dim<T, 2>(p->method, p->sp.ns, a, p->stream);
-    default: return spread_dim<T, 3>(p->method, p->sp.ns, a, p->stream);
-  }
-}
-
-template <typename T>
-static cudaError_t run_interp(Plan<T>* p, const SpreadArgs<T>& a) {
-  switch (p->dim) {
-    case 1: return interp_dim<T, 1>(p->method, p->sp.ns, a, p->stream);
-    case 2: return interp_dim<T, 2>(p->method, p->sp.ns, a, p->stream);
-    default: return interp_dim<T, 3>(p->method, p->sp.ns, a, p->stream);
-  }
+  return select_layout(p);
 }
 
 static int max_smem_optin(int device) {
@@ -595,6 +440,362 @@ static void fill_info(const Plan<T>* p, cufinufft_plan_info* info) {
   info->es_c = p->sp.c;
 }
 
+// ---------------------------------------------------------------------------
+// Layout changes and autotuning (extensions).
+
+// Reallocate the bin tables for nbins bins.
+template <typename T>
+static int alloc_bins(Plan<T>* p, int nbins) {
+  cudaFree(p->count);
+  cudaFree(p->start);
+  cudaFree(p->sub_start);
+  cudaFree(p->scan_tmp);
+  p->count = p->start = p->sub_start = p->scan_tmp = nullptr;
+  CFG_CUDA(cudaMalloc(&p->count, sizeof(int) * (size_t)nbins));
+  CFG_CUDA(cudaMalloc(&p->start, sizeof(int) * ((size_t)nbins + 1)));
+  CFG_CUDA(cudaMalloc(&p->sub_start, sizeof(int) * ((size_t)nbins + 1)));
+  CFG_CUDA(cudaMalloc(&p->scan_tmp, sizeof(int) * (size_t)scan_tmp_ints(nbins)));
+  return 0;
+}
+
+// Subproblem tables of the current layout (method 2): one readback of the
+// total, as in setpts.
+template <typename T>
+static int build_subproblems(Plan<T>* p) {
+  p->nsub = 0;
+  if (p->M == 0) return 0;
+  const int ms = p->opts.gpu_maxsubprobsize;
+  CFG_CUDA(launch_scan(p->count, p->sub_start, p->nbins, 1, ms, p->scan_tmp, p->stream));
+  CFG_CUDA(cudaMemcpyAsync(p->h_total, p->sub_start + p->nbins, sizeof(int), cudaMemcpyDeviceToHost,
+                           p->stream));
+  CFG_CUDA(cudaStreamSynchronize(p->stream));
+  const int nsub = *p->h_total;
+  if ((size_t)nsub > p->cap_sub) {
+    cudaFree(p->sub_to_bin);
+    p->sub_to_bin = nullptr;
+    p->cap_sub = 0;
+    CFG_CUDA(cudaMalloc(&p->sub_to_bin, sizeof(int) * (size_t)nsub));
+    p->cap_sub = nsub;
+  }
+  CFG_CUDA(launch_sub_to_bin(p->sub_start, p->nbins, nsub, p->sub_to_bin, p->stream));
+  p->nsub = nsub;
+  return 0;
+}
+
+// Switch a plan with points set to another method / bin size / subproblem
+// cap by re-sorting its stored points (the caller's coordinates are not
+// needed).  Results are unchanged; only the work schedule moves.
+template <typename T>
+static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub) {
+  if (!p->planned) return CUFINUFFT_ERR_GENERIC;
+  if (method != 1 && method != 2) return CUFINUFFT_ERR_METHOD;
+  if (method == 2 && p->type == 2 && p->dim == 1) return CUFINUFFT_ERR_METHOD;
+  if (method == 2 && maxsub <= 0) return CUFINUFFT_ERR_ARG;
+  int bs[3], nb[3];
+  long long nbins = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (k < p->dim) {
+      if (bsz[k] <= 0) return CUFINUFFT_ERR_ARG;
+      bs[k] = std::min(bsz[k], p->nf[k]);
+      nb[k] = (p->nf[k] + bs[k] - 1) / bs[k];
+    } else {
+      bs[k] = 1;
+      nb[k] = 1;
+    }
+    nbins *= nb[k];
+  }
+  if (nbins > (1LL << 24)) return CUFINUFFT_ERR_ARG;
+  if (method == 2 && tile_cells(p->dim, p->sp.ns, bs) * sizeof(cplx_t<T>) >
+                         (size_t)max_smem_optin(p->device))
+    return CUFINUFFT_ERR_SHMEM;
+  int e = alloc_bins(p, (int)nbins);
+  if (e) return e;
+  if (p->pts_set && p->M > 0) {
+    // fresh arrays for the re-sorted points
+    int* idx = nullptr;
+    int* i0[3] = {nullptr, nullptr, nullptr};
+    T* d[3] = {nullptr, nullptr, nullptr};
+    CFG_CUDA(cudaMalloc(&idx, sizeof(int) * p->capM));
+    for (int k = 0; k < p->dim; ++k) {
+      CFG_CUDA(cudaMalloc(&i0[k], sizeof(int) * p->capM));
+      CFG_CUDA(cudaMalloc(&d[k], sizeof(T) * p->capM));
+    }
+    RebinArgs<T> a;
+    std::memset(&a, 0, sizeof(a));
+    a.dim = p->dim;
+    a.M = p->M;
+    for (int k = 0; k < 3; ++k) {
+      a.bs[k] = bs[k];
+      a.nb[k] = nb[k];
+      a.src_i0[k] = p->i0[k];
+      a.src_d[k] = p->d[k];
+      a.i0[k] = i0[k];
+      a.d[k] = d[k];
+    }
+    a.src_idx = p->idx;
+    a.idx = idx;
+    a.count = p->count;
+    a.rank = p->rank;
+    a.start = p->start;
+    CFG_CUDA(cudaMemsetAsync(p->count, 0, sizeof(int) * (size_t)nbins, p->stream));
+    CFG_CUDA(launch_rebin_count<T>(a, p->stream));
+    CFG_CUDA(launch_scan(p->count, p->start, (int)nbins, 0, 1, p->scan_tmp, p->stream));
+    CFG_CUDA(launch_rebin_permute<T>(a, p->stream));
+    CFG_CUDA(cudaStreamSynchronize(p->stream));
+    cudaFree(p->idx);
+    p->idx = idx;
+    for (int k = 0; k < p->dim; ++k) {
+      cudaFree(p->i0[k]);
+      cudaFree(p->d[k]);
+      p->i0[k] = i0[k];
+      p->d[k] = d[k];
+    }
+  }
+  p->method = method;
+  p->sort = 1;
+  p->opts.gpu_method = method;
+  p->opts.gpu_sort = 1;
+  for (int k = 0; k < 3; ++k) {
+    p->bs[k] = bs[k];
+    p->nb[k] = nb[k];
+  }
+  p->opts.gpu_binsizex = bs[0];
+  p->opts.gpu_binsizey = bs[1];
+  p->opts.gpu_binsizez = bs[2];
+  if (method == 2) p->opts.gpu_maxsubprobsize = maxsub;
+  p->nbins = (int)nbins;
+  p->nsub = 0;
+  if (method == 2 && p->pts_set) {
+    e = build_subproblems(p);
+    if (e) return e;
+  }
+  return 0;
+}
+
+// Device time (ms) of the plan's spread (type 1) or interp (type 2) stage for
+// one batch, median of `reps` runs after one warm-up, on synthetic values.
+template <typename T>
+static int time_stage(Plan<T>* p, cplx_t<T>* scratch, int reps, float* ms) {
+  SpreadArgs<T> a = spread_args(p);
+  a.ntr = p->maxbatch;
+  cudaEvent_t e0, e1;
+  CFG_CUDA(cudaEventCreate(&e0));
+  CFG_CUDA(cudaEventCreate(&e1));
+  std::vector<float> t;
+  for (int r = 0; r <= reps; ++r) {
+    CFG_CUDA(cudaEventRecord(e0, p->stream));
+    if (p->type == 1) {
+      a.c_in = scratch;
+      a.fw = p->fw;
+      CFG_CUDA(run_spread(p, a));
+    } else {
+      a.fw_in = p->fw;
+      a.c_out = scratch;
+      CFG_CUDA(run_interp(p, a));
+    }
+    CFG_CUDA(cudaEventRecord(e1, p->stream));
+    CFG_CUDA(cudaEventSynchronize(e1));
+    float v = 0;
+    CFG_CUDA(cudaEventElapsedTime(&v, e0, e1));
+    if (r > 0) t.push_back(v);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  std::sort(t.begin(), t.end());
+  *ms = t[t.size() / 2];
+  return 0;
+}
+
+// The layout classes the autotuner times and the learned selector chooses
+// among, in a fixed order: 0-2 method 1 with small / medium / large bins,
+// 3-8 method 2 with small / medium / large bins x subproblem cap 256 / 1024.
+// Bin shapes per dimension: 1D 256 / 1024 / 4096; 2D 16^2 / 32^2 / 64^2;
+// 3D 8x8x8 / 16x16x2 / 16x16x4 (clamped to the fine grid).  A class the plan
+// cannot run (method 2 for 1D type 2, a tile beyond shared memory) has
+// ms = -2.
+constexpr int kLayoutClasses = 9;
+
+template <typename T>
+static cufinufft_tune_entry layout_class(const Plan<T>* p, int cls) {
+  static const int shapes[3][3][3] = {{{256, 1, 1}, {1024, 1, 1}, {4096, 1, 1}},
+                                      {{16, 16, 1}, {32, 32, 1}, {64, 64, 1}},
+                                      {{8, 8, 8}, {16, 16, 2}, {16, 16, 4}}};
+  cufinufft_tune_entry e;
+  e.method = cls < 3 ? 1 : 2;
+  const int shape = cls < 3 ? cls : (cls - 3) / 2;
+  const int* sh = shapes[p->dim - 1][shape];
+  e.binsizex = std::min(sh[0], p->nf[0]);
+  e.binsizey = p->dim > 1 ? std::min(sh[1], p->nf[1]) : 1;
+  e.binsizez = p->dim > 2 ? std::min(sh[2], p->nf[2]) : 1;
+  e.maxsubprobsize = cls < 3 ? 1024 : ((cls - 3) % 2 == 0 ? 256 : 1024);
+  e.ms = -1.f;
+  int bs[3] = {e.binsizex, e.binsizey, e.binsizez};
+  if (e.method == 2 && p->type == 2 && p->dim == 1) e.ms = -2.f;
+  if (e.method == 2 && tile_cells(p->dim, p->sp.ns, bs) * sizeof(cplx_t<T>) >
+                           (size_t)max_smem_optin(p->device))
+    e.ms = -2.f;
+  return e;
+}
+
+template <typename T>
+static std::vector<cufinufft_tune_entry> tune_candidates(const Plan<T>* p) {
+  std::vector<cufinufft_tune_entry> c;
+  for (int k = 0; k < kLayoutClasses; ++k) c.push_back(layout_class(p, k));
+  return c;
+}
+
+template <typename T>
+static int autotune_impl(Plan<T>* p, cufinufft_tune_entry* out, int max_out, int* n_out) {
+  if (!p->planned || !p->pts_set) return CUFINUFFT_ERR_GENERIC;
+  std::vector<cufinufft_tune_entry> cand = tune_candidates(p);
+  if (n_out) *n_out = 0;
+  if (p->M == 0) return 0;
+  cplx_t<T>* scratch = nullptr;
+  CFG_CUDA(cudaMalloc(&scratch, sizeof(cplx_t<T>) * (size_t)p->M * p->maxbatch));
+  // nonzero synthetic strengths/values (a zero tile would be skipped)
+  CFG_CUDA(cudaMemsetAsync(scratch, 0x3f, sizeof(cplx_t<T>) * (size_t)p->M * p->maxbatch, p->stream));
+  if (p->type == 2)
+    CFG_CUDA(cudaMemsetAsync(p->fw, 0x3f, sizeof(cplx_t<T>) * (size_t)grid_cells(p) * p->maxbatch,
+                             p->stream));
+  int best = -1;
+  for (size_t i = 0; i < cand.size(); ++i) {
+    if (cand[i].ms == -2.f) continue;  // not runnable for this plan
+    int bs[3] = {cand[i].binsizex, cand[i].binsizey, cand[i].binsizez};
+    int e = set_layout_impl(p, cand[i].method, bs, cand[i].maxsubprobsize);
+    if (e) continue;
+    if (p->type == 1)
+      CFG_CUDA(cudaMemsetAsync(p->fw, 0, sizeof(cplx_t<T>) * (size_t)grid_cells(p) * p->maxbatch,
+                               p->stream));
+    float ms = 0;
+    e = time_stage(p, scratch, 3, &ms);
+    if (e) {
+      cudaFree(scratch);
+      return e;
+    }
+    cand[i].ms = ms;
+    if (best < 0 || ms < cand[best].ms) best = (int)i;
+  }
+  cudaFree(scratch);
+  if (best < 0) return CUFINUFFT_ERR_GENERIC;
+  int bs[3] = {cand[best].binsizex, cand[best].binsizey, cand[best].binsizez};
+  int e = set_layout_impl(p, cand[best].method, bs, cand[best].maxsubprobsize);
+  if (e) return e;
+  int n = 0;
+  if (out) {
+    // the chosen layout first, then every candidate tried
+    out[n++] = cand[best];
+    for (size_t i = 0; i < cand.size() && n < max_out; ++i) out[n++] = cand[i];
+  }
+  if (n_out) *n_out = n;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Features and the learned selector.
+
+template <typename T>
+static int features_impl(Plan<T>* p, float* f) {
+  if (!p->planned || !p->pts_set) return CUFINUFFT_ERR_GENERIC;
+  int fb[3] = {1, 1, 1}, nb[3] = {1, 1, 1};
+  long long nbins = 1;
+  for (int k = 0; k < p->dim; ++k) {
+    fb[k] = std::min(p->dim == 1 ? 64 : (p->dim == 2 ? 16 : 8), p->nf[k]);
+    nb[k] = (p->nf[k] + fb[k] - 1) / fb[k];
+    nbins *= nb[k];
+  }
+  std::vector<int> h((size_t)nbins, 0);
+  if (p->M > 0) {
+    int* counts = nullptr;
+    CFG_CUDA(cudaMalloc(&counts, sizeof(int) * (size_t)nbins));
+    CFG_CUDA(cudaMemsetAsync(counts, 0, sizeof(int) * (size_t)nbins, p->stream));
+    const int* i0[3] = {p->i0[0], p->i0[1], p->i0[2]};
+    cudaError_t e = launch_feature_count(p->dim, p->M, i0, fb, nb, counts, p->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(h.data(), counts, sizeof(int) * (size_t)nbins, cudaMemcpyDeviceToHost,
+                          p->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+    cudaFree(counts);
+    CFG_CUDA(e);
+  }
+  double sum = 0, sumsq = 0, mx = 0, occ = 0, sq_occ = 0;
+  for (int c : h) {
+    sum += c;
+    sumsq += (double)c * c;
+    if (c > mx) mx = c;
+    if (c > 0) {
+      occ += 1;
+      sq_occ += (double)c * c;
+    }
+  }
+  const double Nf = (double)grid_cells(p);
+  const double Nm = (double)p->N[0] * p->N[1] * p->N[2];
+  const double mean_all = sum / (double)nbins;
+  const double mean_occ = occ > 0 ? sum / occ : 0.0;
+  const double var_occ = occ > 0 ? std::max(0.0, sq_occ / occ - mean_occ * mean_occ) : 0.0;
+  f[0] = (float)p->dim;
+  f[1] = (float)p->type;
+  f[2] = is_single<T>() ? 1.f : 0.f;
+  f[3] = (float)p->sp.ns;
+  f[4] = (float)std::log2((double)p->M + 1.0);
+  f[5] = (float)std::log2(Nm);
+  f[6] = (float)std::log2(Nf);
+  f[7] = (float)std::log2(((double)p->M + 1.0) / Nf);
+  f[8] = (float)std::log2((double)p->ntransf);
+  f[9] = (float)(occ / (double)nbins);
+  f[10] = (float)(mean_occ > 0 ? std::sqrt(var_occ) / mean_occ : 0.0);
+  f[11] = (float)(mean_all > 0 ? std::log2(mx / mean_all) : 0.0);
+  f[12] = (float)std::log2(mean_occ + 1.0);
+  f[13] = (float)(sum > 0 ? std::log2((double)nbins * sumsq / (sum * sum)) : 0.0);
+  return 0;
+}
+
+template <typename T>
+static int apply_layout_class(Plan<T>* p, int cls);
+
+// gpu_method 0 with a trained network: predict the nine classes' relative
+// times from the plan's features and switch to the fastest runnable one.
+template <typename T>
+static int select_layout(Plan<T>* p) {
+  if (!kSelectorTrained || !p->auto_method || !p->pts_set || p->M == 0) return 0;
+  float f[CUFINUFFT_MLP_FEATURES];
+  int e = features_impl(p, f);
+  if (e) return e;
+  for (int k = 0; k < CUFINUFFT_MLP_FEATURES; ++k) f[k] = (f[k] - kSelMean[k]) / kSelStd[k];
+  const int B = 1, Hd = CUFINUFFT_MLP_HIDDEN, K = CUFINUFFT_MLP_CLASSES;
+  const size_t nfl = CUFINUFFT_MLP_PARAMS + CUFINUFFT_MLP_FEATURES + K + 2 * B * Hd;
+  if (p->sel_buf == nullptr) {
+    CFG_CUDA(cudaMalloc(&p->sel_buf, sizeof(float) * nfl));
+    CFG_CUDA(cudaMemcpyAsync(p->sel_buf, kSelParams, sizeof(float) * CUFINUFFT_MLP_PARAMS,
+                             cudaMemcpyHostToDevice, p->stream));
+  }
+  float* params = p->sel_buf;
+  float* X = params + CUFINUFFT_MLP_PARAMS;
+  float* Y = X + CUFINUFFT_MLP_FEATURES;
+  float* work = Y + K;
+  CFG_CUDA(cudaMemcpyAsync(X, f, sizeof(f), cudaMemcpyHostToDevice, p->stream));
+  if (cufinufft_mlp_forward(params, X, B, Y, work, p->stream) != 0) return CUFINUFFT_ERR_CUDA;
+  float y[CUFINUFFT_MLP_CLASSES];
+  CFG_CUDA(cudaMemcpyAsync(y, Y, sizeof(y), cudaMemcpyDeviceToHost, p->stream));
+  CFG_CUDA(cudaStreamSynchronize(p->stream));
+  int best = -1;
+  for (int k = 0; k < K; ++k) {
+    cufinufft_tune_entry c = tune_candidates(p)[k];
+    if (c.ms == -2.f) continue;
+    if (best < 0 || y[k] < y[best]) best = k;
+  }
+  if (best < 0) return 0;
+  return apply_layout_class(p, best);
+}
+
+template <typename T>
+static int apply_layout_class(Plan<T>* p, int cls) {
+  if (cls < 0 || cls >= kLayoutClasses) return CUFINUFFT_ERR_ARG;
+  cufinufft_tune_entry c = tune_candidates(p)[cls];
+  if (c.ms == -2.f) return CUFINUFFT_ERR_METHOD;
+  int bs[3] = {c.binsizex, c.binsizey, c.binsizez};
+  return set_layout_impl(p, c.method, bs, c.maxsubprobsize);
+}
+
 template <typename T, typename H>
 static int makeplan_entry(int type, int dim, int* nmodes, int iflag, int ntransf, double tol,
                           int maxbatchsize, H** plan, cufinufft_opts* opts) {
@@ -623,12 +824,6 @@ static int makeplan_entry(int type, int dim, int* nmodes, int iflag, int ntransf
 
 }  // namespace cfg
 
-struct cufinufft_plan_s {
-  cfg::Plan<double> p;
-};
-struct cufinufftf_plan_s {
-  cfg::Plan<float> p;
-};
 
 using cfg::DeviceGuard;
 
@@ -673,6 +868,20 @@ static int stage_times_entry(H* h, double* ms, long long* batches, int reset) {
     h->p.stage_batches = 0;
   }
   return 0;
+}
+
+template <typename H>
+static int set_layout_entry(H* h, int method, int bx, int by, int bz, int maxsub) {
+  if (!h) return CUFINUFFT_ERR_GENERIC;
+  DeviceGuard g(h->p.device);
+  int bs[3] = {bx, by, bz};
+  return cfg::set_layout_impl(&h->p, method, bs, maxsub);
+}
+template <typename H>
+static int autotune_entry(H* h, cufinufft_tune_entry* out, int max_out, int* n_out) {
+  if (!h) return CUFINUFFT_ERR_GENERIC;
+  DeviceGuard g(h->p.device);
+  return cfg::autotune_impl(&h->p, out, max_out, n_out);
 }
 
 extern "C" {
@@ -749,6 +958,40 @@ int cufinufft_stage_times(cufinufft_plan plan, double* ms, long long* batches, i
 }
 int cufinufftf_stage_times(cufinufftf_plan plan, double* ms, long long* batches, int reset) {
   return stage_times_entry(plan, ms, batches, reset);
+}
+
+int cufinufft_set_layout(cufinufft_plan plan, int method, int bx, int by, int bz, int maxsub) {
+  return set_layout_entry(plan, method, bx, by, bz, maxsub);
+}
+int cufinufftf_set_layout(cufinufftf_plan plan, int method, int bx, int by, int bz, int maxsub) {
+  return set_layout_entry(plan, method, bx, by, bz, maxsub);
+}
+int cufinufft_autotune(cufinufft_plan plan, cufinufft_tune_entry* out, int max_out, int* n_out) {
+  return autotune_entry(plan, out, max_out, n_out);
+}
+int cufinufftf_autotune(cufinufftf_plan plan, cufinufft_tune_entry* out, int max_out, int* n_out) {
+  return autotune_entry(plan, out, max_out, n_out);
+}
+
+int cufinufft_features(cufinufft_plan plan, float* features) {
+  if (!plan || !features) return CUFINUFFT_ERR_GENERIC;
+  DeviceGuard g(plan->p.device);
+  return cfg::features_impl(&plan->p, features);
+}
+int cufinufftf_features(cufinufftf_plan plan, float* features) {
+  if (!plan || !features) return CUFINUFFT_ERR_GENERIC;
+  DeviceGuard g(plan->p.device);
+  return cfg::features_impl(&plan->p, features);
+}
+int cufinufft_set_layout_class(cufinufft_plan plan, int cls) {
+  if (!plan) return CUFINUFFT_ERR_GENERIC;
+  DeviceGuard g(plan->p.device);
+  return cfg::apply_layout_class(&plan->p, cls);
+}
+int cufinufftf_set_layout_class(cufinufftf_plan plan, int cls) {
+  if (!plan) return CUFINUFFT_ERR_GENERIC;
+  DeviceGuard g(plan->p.device);
+  return cfg::apply_layout_class(&plan->p, cls);
 }
 
 int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info) {

@@ -1,0 +1,18 @@
+// Multi-plan spread/interp kernels of double batches.
+#include "batch.cuh"
+
+namespace cfg {
+
+template <typename T>
+cudaError_t batch_spreadinterp(Batch<T>* b) {
+  const int n = (int)b->plans.size();
+  switch (b->dim) {
+    case 1: return batch_spreadinterp_dim<T, 1>(b, n, b->ntasks);
+    case 2: return batch_spreadinterp_dim<T, 2>(b, n, b->ntasks);
+    default: return batch_spreadinterp_dim<T, 3>(b, n, b->ntasks);
+  }
+}
+
+template cudaError_t batch_spreadinterp<double>(Batch<double>*);
+
+}  // namespace cfg

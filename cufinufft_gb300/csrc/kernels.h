@@ -34,6 +34,30 @@ template <typename T> cudaError_t launch_bin_count(const PlaceArgs<T>& a, cudaSt
 template <typename T> cudaError_t launch_permute(const PlaceArgs<T>& a, cudaStream_t s);
 template <typename T> cudaError_t launch_place_unsorted(const PlaceArgs<T>& a, cudaStream_t s);
 
+// Re-binning of already placed points (no caller coordinates needed): the
+// bin of a point depends only on its first taps i0, so a new bin layout is a
+// counting sort of the stored arrays into fresh ones.
+template <typename T> struct RebinArgs {
+  int dim, M;
+  int bs[3], nb[3];
+  const int* src_idx;
+  const int* src_i0[3];
+  const T* src_d[3];
+  int* idx;
+  int* i0[3];
+  T* d[3];
+  int* count;      // [nbins], zeroed before rebin_count
+  int* rank;       // [M]
+  const int* start;
+};
+template <typename T> cudaError_t launch_rebin_count(const RebinArgs<T>& a, cudaStream_t s);
+template <typename T> cudaError_t launch_rebin_permute(const RebinArgs<T>& a, cudaStream_t s);
+
+// Point counts over fixed feature bins (fb cells per axis) from the stored
+// first taps; counts must be zeroed.
+cudaError_t launch_feature_count(int dim, int M, const int* const i0[3], const int fb[3],
+                                 const int nb[3], int* counts, cudaStream_t s);
+
 // Exclusive scan of n ints: out[0..n] (out[n] = total).  mode 0 scans the
 // values, mode 1 scans ceil(v / div).  tmp needs scan_tmp_ints(n) ints.
 int scan_tmp_ints(int n);

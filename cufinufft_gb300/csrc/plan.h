@@ -1,0 +1,184 @@
+// plan.h -- the plan object shared by the C ABI (api.cu) and the
+// multi-plan batch (batch.cu), with small helpers both use.
+#pragma once
+
+#include <cufft.h>
+
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/cufinufft.h"
+#include "kernels.h"
+#include "planner.h"
+
+namespace cfg {
+
+template <typename T> struct Plan {
+  using C = cplx_t<T>;
+  int type = 0, dim = 0;
+  int N[3] = {1, 1, 1};
+  int nf[3] = {1, 1, 1};
+  int ntransf = 1, maxbatch = 1, iflag = 1;
+  cufinufft_opts opts;
+  SpreaderParams sp{};
+  int method = 0;  // method run: 1 (NU-point driven) or 2 (subproblem); 0 = invalid
+  int variant = 0; // kernel family: 0 default, 1 one thread per point, 2 warp-cooperative
+  bool auto_method = false;  // gpu_method 0: chosen by the library
+  float* sel_buf = nullptr;  // selector network parameters and scratch (device)
+  int sort = 1;
+  int bs[3] = {1, 1, 1}, nb[3] = {1, 1, 1};
+  int nbins = 1;
+  int device = 0;
+  int M = 0, nsub = 0;
+  bool planned = false, pts_set = false;
+  cudaStream_t own = nullptr, stream = nullptr;
+  cufftHandle fft = 0, fft_rem = 0;
+  bool have_fft = false, have_fft_rem = false;
+  int rem = 0;
+  C* fw = nullptr;
+  T* fac[3] = {nullptr, nullptr, nullptr};
+  std::vector<T> horner;  // fitted kernel polynomials (kerevalmeth 1), [k][j]
+  T* horner_d = nullptr;  // device copy of the same
+  // sorted points and bin tables
+  int* idx = nullptr;
+  int* i0[3] = {nullptr, nullptr, nullptr};
+  T* d[3] = {nullptr, nullptr, nullptr};
+  int* rank = nullptr;
+  size_t capM = 0;
+  int* count = nullptr;
+  int* start = nullptr;
+  int* sub_start = nullptr;
+  int* scan_tmp = nullptr;
+  int* sub_to_bin = nullptr;
+  size_t cap_sub = 0;
+  int* h_total = nullptr;  // pinned readback of the subproblem count
+  // stage timing (extension): events recorded around each stage of execute
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;   // free events
+  std::vector<cudaEvent_t> ev_live;   // groups of 4 per batch, not yet read
+  double stage_ms[3] = {0, 0, 0};     // spread|interp, fft, deconv|amplify
+  long long stage_batches = 0;
+};
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    ok = cudaSetDevice(dev) == cudaSuccess;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+#define CFG_CUDA(call)                                             \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) {                                       \
+      fprintf(stderr, "cufinufft: %s failed: %s\n", #call, cudaGetErrorString(e_)); \
+      return e_ == cudaErrorMemoryAllocation ? CUFINUFFT_ERR_ALLOC : CUFINUFFT_ERR_CUDA; \
+    }                                                              \
+  } while (0)
+
+#define CFG_CUFFT(call)                                            \
+  do {                                                             \
+    cufftResult r_ = (call);                                       \
+    if (r_ != CUFFT_SUCCESS) {                                     \
+      fprintf(stderr, "cufinufft: %s failed: cufftResult %d\n", #call, (int)r_); \
+      return r_ == CUFFT_ALLOC_FAILED ? CUFINUFFT_ERR_ALLOC : CUFINUFFT_ERR_CUFFT; \
+    }                                                              \
+  } while (0)
+
+template <typename T> constexpr bool is_single() { return sizeof(T) == 4; }
+
+template <typename T> cufftType fft_type();
+template <> inline cufftType fft_type<float>() { return CUFFT_C2C; }
+template <> inline cufftType fft_type<double>() { return CUFFT_Z2Z; }
+
+inline cufftResult fft_exec(cufftHandle h, float2* data, int dir) {
+  return cufftExecC2C(h, (cufftComplex*)data, (cufftComplex*)data, dir);
+}
+inline cufftResult fft_exec(cufftHandle h, double2* data, int dir) {
+  return cufftExecZ2Z(h, (cufftDoubleComplex*)data, (cufftDoubleComplex*)data, dir);
+}
+
+template <typename T> inline long long grid_cells(const Plan<T>* p) {
+  return (long long)p->nf[0] * p->nf[1] * p->nf[2];
+}
+
+template <typename T>
+inline AxisMap<T> axis_map(int nf, int ns) {
+  AxisMap<T> a;
+  const double S = (double)nf / (2.0 * M_PI);
+  a.s_hi = (T)S;
+  a.s_lo = (T)(S - (double)a.s_hi);
+  a.o_lo = (T)(1.5 * nf);
+  a.o_mid = (T)(0.5 * nf);
+  a.o_hi = (T)(-0.5 * nf);
+  a.half_int = ns / 2;
+  a.half_frac = (ns % 2) ? T(0.5) : T(0);
+  a.nf = nf;
+  return a;
+}
+
+template <typename T>
+inline SpreadArgs<T> spread_args(Plan<T>* p) {
+  SpreadArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.pts.idx = p->idx;
+  for (int k = 0; k < 3; ++k) {
+    a.pts.i0[k] = p->i0[k];
+    a.pts.d[k] = p->d[k];
+    a.bins.bs[k] = p->bs[k];
+    a.bins.nb[k] = p->nb[k];
+    a.g.nf[k] = p->nf[k];
+  }
+  a.pts.M = p->M;
+  a.bins.nbins = p->nbins;
+  a.bins.count = p->count;
+  a.bins.start = p->start;
+  a.bins.sub_start = p->sub_start;
+  a.bins.sub_to_bin = p->sub_to_bin;
+  a.bins.nsub = p->nsub;
+  a.bins.maxsub = p->opts.gpu_maxsubprobsize;
+  a.kc.beta = (T)p->sp.beta;
+  a.kc.c = (T)p->sp.c;
+  a.kc.horner = p->horner.empty() ? 0 : 1;
+  a.kc.coef_g = p->horner_d;
+  for (size_t k = 0; k < p->horner.size() && k < (size_t)(kMaxHornerRows * kMaxNS); ++k)
+    a.kc.coef[k] = p->horner[k];
+  a.g.Nf = grid_cells(p);
+  a.M = p->M;
+  a.variant = p->variant;
+  return a;
+}
+
+template <typename T>
+inline cudaError_t run_spread(Plan<T>* p, const SpreadArgs<T>& a) {
+  switch (p->dim) {
+    case 1: return spread_dim<T, 1>(p->method, p->sp.ns, a, p->stream);
+    case 2: return spread_dim<T, 2>(p->method, p->sp.ns, a, p->stream);
+    default: return spread_dim<T, 3>(p->method, p->sp.ns, a, p->stream);
+  }
+}
+
+template <typename T>
+inline cudaError_t run_interp(Plan<T>* p, const SpreadArgs<T>& a) {
+  switch (p->dim) {
+    case 1: return interp_dim<T, 1>(p->method, p->sp.ns, a, p->stream);
+    case 2: return interp_dim<T, 2>(p->method, p->sp.ns, a, p->stream);
+    default: return interp_dim<T, 3>(p->method, p->sp.ns, a, p->stream);
+  }
+}
+
+}  // namespace cfg
+
+struct cufinufft_plan_s {
+  cfg::Plan<double> p;
+};
+struct cufinufftf_plan_s {
+  cfg::Plan<float> p;
+};

@@ -122,6 +122,107 @@ template cudaError_t launch_place_unsorted<float>(const PlaceArgs<float>&, cudaS
 template cudaError_t launch_place_unsorted<double>(const PlaceArgs<double>&, cudaStream_t);
 
 // ---------------------------------------------------------------------------
+// Re-binning from stored first taps.
+template <typename T>
+__device__ __forceinline__ int stored_bin(const RebinArgs<T>& a, int i) {
+  int b = 0, mul = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (k < a.dim) {
+      b += mul * (a.src_i0[k][i] / a.bs[k]);
+      mul *= a.nb[k];
+    }
+  }
+  return b;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPlaceThreads) k_rebin_count(RebinArgs<T> a) {
+  const int lane = threadIdx.x & 31;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < a.M; base += stride) {
+    const long long ii = base + threadIdx.x;
+    const bool active = ii < a.M;
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!active) continue;
+    const int i = (int)ii;
+    const int b = stored_bin(a, i);
+    const unsigned peers = __match_any_sync(act, b);
+    const int leader = __ffs(peers) - 1;
+    int first = 0;
+    if (lane == leader) first = atomicAdd(&a.count[b], __popc(peers));
+    first = __shfl_sync(peers, first, leader);
+    a.rank[i] = first + __popc(peers & ((1u << lane) - 1u));
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPlaceThreads) k_rebin_permute(RebinArgs<T> a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += gridDim.x * blockDim.x) {
+    const int pos = a.start[stored_bin(a, i)] + a.rank[i];
+    a.idx[pos] = a.src_idx[i];
+    for (int k = 0; k < 3; ++k) {
+      if (k < a.dim) {
+        a.i0[k][pos] = a.src_i0[k][i];
+        a.d[k][pos] = a.src_d[k][i];
+      }
+    }
+  }
+}
+
+template <typename T> cudaError_t launch_rebin_count(const RebinArgs<T>& a, cudaStream_t s) {
+  if (a.M == 0) return cudaSuccess;
+  k_rebin_count<T><<<place_grid(a.M), kPlaceThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+template <typename T> cudaError_t launch_rebin_permute(const RebinArgs<T>& a, cudaStream_t s) {
+  if (a.M == 0) return cudaSuccess;
+  k_rebin_permute<T><<<place_grid(a.M), kPlaceThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+template cudaError_t launch_rebin_count<float>(const RebinArgs<float>&, cudaStream_t);
+template cudaError_t launch_rebin_count<double>(const RebinArgs<double>&, cudaStream_t);
+template cudaError_t launch_rebin_permute<float>(const RebinArgs<float>&, cudaStream_t);
+template cudaError_t launch_rebin_permute<double>(const RebinArgs<double>&, cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Occupancy counts for the selector's features.
+struct FeatureArgs {
+  const int* i0[3];
+  int fb[3], nb[3];
+  int dim, M;
+  int* counts;
+};
+
+__global__ void k_feature_count(FeatureArgs a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += gridDim.x * blockDim.x) {
+    int b = 0, mul = 1;
+    for (int k = 0; k < 3; ++k) {
+      if (k < a.dim) {
+        b += mul * (a.i0[k][i] / a.fb[k]);
+        mul *= a.nb[k];
+      }
+    }
+    atomicAdd(&a.counts[b], 1);
+  }
+}
+
+cudaError_t launch_feature_count(int dim, int M, const int* const i0[3], const int fb[3],
+                                 const int nb[3], int* counts, cudaStream_t s) {
+  if (M == 0) return cudaSuccess;
+  FeatureArgs a;
+  for (int k = 0; k < 3; ++k) {
+    a.i0[k] = i0[k];
+    a.fb[k] = fb[k];
+    a.nb[k] = nb[k];
+  }
+  a.dim = dim;
+  a.M = M;
+  a.counts = counts;
+  k_feature_count<<<place_grid(M), kPlaceThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Exclusive scan: 1024 threads x 4 items per block; block totals are scanned
 // by one block (up to 4096 blocks, i.e. 16.7M entries), then added back.
 constexpr int kScanThreads = 1024;

@@ -314,6 +314,9 @@ k_interp_sm(SpreadArgs<T> a) {
 template <int NS> constexpr int lanes_per_point() {
   return NS <= 2 ? 2 : (NS <= 4 ? 4 : (NS <= 8 ? 8 : 16));
 }
+// Spreading needs no butterfly, so its lane groups are exactly ns wide:
+// floor(32/ns) points per warp step (5 at ns = 6 instead of 4).
+template <int NS> constexpr int spread_lanes() { return NS; }
 
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
@@ -382,7 +385,7 @@ __global__ void __launch_bounds__(kSpreadThreads)
 k_spread_gm_wc(SpreadArgs<T> a) {
   using C = cplx_t<T>;
   constexpr int HD = horner_degree<T>(NS);
-  constexpr int L = lanes_per_point<NS>();
+  constexpr int L = spread_lanes<NS>();
   constexpr int PPW = 32 / L;
   constexpr int NY = DIM > 1 ? NS : 1;
   constexpr int NZ = DIM > 2 ? NS : 1;
@@ -394,7 +397,7 @@ k_spread_gm_wc(SpreadArgs<T> a) {
   const int nf0 = a.g.nf[0], nf1 = a.g.nf[1], nf2 = a.g.nf[2];
   for (long long base = wid * PPW; base < a.M; base += nw * PPW) {
     const long long pl = base + g;
-    const bool valid = pl < a.M;
+    const bool valid = g < PPW && pl < a.M;
     const int p = valid ? (int)pl : a.M - 1;
     const int xj = wrap_idx(a.pts.i0[0][p] + jj, nf0);
     const T kx = kernel_tap<T, NS, HD>(a.pts.d[0][p], jj, a.kc);
@@ -423,20 +426,46 @@ k_spread_gm_wc(SpreadArgs<T> a) {
   }
 }
 
+// The tile is held as two planes (real parts, then imaginary parts): the ns
+// taps of a point's row are then ns consecutive words of one plane, so a
+// warp's shared atomics touch ns consecutive banks per point instead of every
+// other bank of 2 ns (interleaved complex), halving bank conflicts.
+template <typename T>
+__device__ __forceinline__ void plane_flush(const T* re, const T* im, cplx_t<T>* grid,
+                                            const SubTile& st, const GridGeom& g) {
+  const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
+  const int rows = st.TY * st.TZ;
+  for (int r = threadIdx.x >> 5; r < rows; r += nwb) {
+    const int iy = r % st.TY, iz = r / st.TY;
+    int gy = st.oy + iy, gz = st.oz + iz;
+    while (gy >= g.nf[1]) gy -= g.nf[1];
+    while (gz >= g.nf[2]) gz -= g.nf[2];
+    cplx_t<T>* dst = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
+    for (int ix = lane; ix < st.TX; ix += 32) {
+      const T vr = re[r * st.TX + ix], vi = im[r * st.TX + ix];
+      if (vr == T(0) && vi == T(0)) continue;
+      int gx = st.ox + ix;
+      while (gx >= g.nf[0]) gx -= g.nf[0];
+      red_add(dst + gx, vr, vi);
+    }
+  }
+}
+
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
 k_spread_sm_wc(SpreadArgs<T> a) {
   using C = cplx_t<T>;
   constexpr int HD = horner_degree<T>(NS);
-  constexpr int L = lanes_per_point<NS>();
+  constexpr int L = spread_lanes<NS>();
   constexpr int PPW = 32 / L;
   constexpr int NY = DIM > 1 ? NS : 1;
   constexpr int NZ = DIM > 2 ? NS : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* tile = reinterpret_cast<C*>(smem_raw);
   const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  T* re = reinterpret_cast<T*>(smem_raw);
+  T* im = re + st.ntile;
   const int t = blockIdx.y;
-  tile_zero<T>(tile, st.ntile);
+  for (int i = threadIdx.x; i < 2 * st.ntile; i += blockDim.x) re[i] = T(0);
   __syncthreads();
   const int lane = threadIdx.x & 31, g = lane / L, j = lane % L;
   const bool tap = j < NS;
@@ -445,7 +474,7 @@ k_spread_sm_wc(SpreadArgs<T> a) {
   const C* cin = a.c_in + (size_t)t * a.M;
   for (int base = warp * PPW; base < st.np; base += nwb * PPW) {
     const int pl = base + g;
-    const bool valid = pl < st.np;
+    const bool valid = g < PPW && pl < st.np;
     const int p = st.p0 + (valid ? pl : st.np - 1);
     const int lx = a.pts.i0[0][p] - st.ox;
     const T kx = kernel_tap<T, NS, HD>(a.pts.d[0][p], jj, a.kc);
@@ -455,7 +484,7 @@ k_spread_sm_wc(SpreadArgs<T> a) {
     if (DIM > 2) { lz = a.pts.i0[2][p] - st.oz; kz = kernel_tap<T, NS, HD>(a.pts.d[2][p], jj, a.kc); }
     const C v = cin[a.pts.idx[p]];
     const T vr = v.x * kx, vi = v.y * kx;
-    C* row0 = tile + (lz * st.TY + ly) * st.TX + lx + jj;
+    const int off0 = (lz * st.TY + ly) * st.TX + lx + jj;
 #pragma unroll 1
     for (int dz = 0; dz < NZ; ++dz) {
       const T kzv = DIM > 2 ? __shfl_sync(0xffffffffu, kz, g * L + dz) : T(1);
@@ -463,12 +492,16 @@ k_spread_sm_wc(SpreadArgs<T> a) {
       for (int dy = 0; dy < NY; ++dy) {
         const T kyv = DIM > 1 ? __shfl_sync(0xffffffffu, ky, g * L + dy) : T(1);
         const T w = kyv * kzv;
-        if (tap && valid) smem_add(row0 + (dz * st.TY + dy) * st.TX, vr * w, vi * w);
+        if (tap && valid) {
+          const int off = off0 + (dz * st.TY + dy) * st.TX;
+          atomicAdd(re + off, vr * w);
+          atomicAdd(im + off, vi * w);
+        }
       }
     }
   }
   __syncthreads();
-  tile_flush<T>(tile, a.fw + (size_t)t * a.g.Nf, st, a.g);
+  plane_flush<T>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g);
 }
 
 template <typename T, int DIM, int NS>
@@ -564,7 +597,7 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
   const bool wc = a.variant != 1;
   if (method == 1) {
     if (wc) {
-      constexpr int PPW = 32 / lanes_per_point<NS>();
+      constexpr int PPW = 32 / spread_lanes<NS>();
       k_spread_gm_wc<T, DIM, NS><<<grid_for(((long long)a.M + PPW - 1) / PPW * 32, kSpreadThreads),
                                    kSpreadThreads, 0, s>>>(a);
     } else {

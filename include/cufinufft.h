@@ -119,6 +119,84 @@ int cufinufftf_set_timing(cufinufftf_plan plan, int on);
 int cufinufft_stage_times(cufinufft_plan plan, double* ms, long long* batches, int reset);
 int cufinufftf_stage_times(cufinufftf_plan plan, double* ms, long long* batches, int reset);
 
+/* Layout and autotuning (no counterpart in the reference).  set_layout
+ * switches a plan whose points are set to another method (1 or 2), bin size
+ * and subproblem cap by re-sorting the stored points -- results do not change,
+ * only the schedule.  autotune times the plan's spread (type 1) or interp
+ * (type 2) stage under the nine layout classes (0-2: method 1 with small,
+ * medium, large bins; 3-8: method 2 with those bins x subproblem cap 256 or
+ * 1024; bins 1D 256/1024/4096, 2D 16^2/32^2/64^2, 3D 8x8x8/16x16x2/16x16x4)
+ * on the plan's own points, keeps the fastest, and reports the chosen entry
+ * first followed by the nine classes in order (ms = -2: not runnable). */
+typedef struct cufinufft_tune_entry {
+  int method, binsizex, binsizey, binsizez, maxsubprobsize;
+  float ms;
+} cufinufft_tune_entry;
+int cufinufft_set_layout(cufinufft_plan plan, int method, int binsizex, int binsizey, int binsizez,
+                         int maxsubprobsize);
+int cufinufftf_set_layout(cufinufftf_plan plan, int method, int binsizex, int binsizey,
+                          int binsizez, int maxsubprobsize);
+int cufinufft_autotune(cufinufft_plan plan, cufinufft_tune_entry* entries, int max_entries,
+                       int* n_entries);
+int cufinufftf_autotune(cufinufftf_plan plan, cufinufft_tune_entry* entries, int max_entries,
+                        int* n_entries);
+
+/* Learned layout selector (no counterpart in the reference).
+ * features() writes CUFINUFFT_MLP_FEATURES numbers describing a plan whose
+ * points are set: 0 dim, 1 type, 2 FP32 (1) or FP64 (0), 3 kernel width,
+ * 4 log2(M+1), 5 log2(modes), 6 log2(fine-grid cells), 7 log2((M+1)/cells),
+ * 8 log2(ntransf), and occupancy statistics of the points over fixed
+ * feature bins (1D 64, 2D 16x16, 3D 8x8x8 cells): 9 fraction of bins that
+ * hold points, 10 coefficient of variation of the counts of those bins,
+ * 11 log2(max / mean count), 12 log2(mean count of occupied bins),
+ * 13 log2(participation ratio nbins * sum c^2 / (sum c)^2).
+ * The network maps standardised features to the predicted log2 time ratio
+ * of each of the nine layout classes (see autotune); its parameters are one
+ * flat FP32 array of CUFINUFFT_MLP_PARAMS floats,
+ *   W1[H][F], b1[H], W2[H][H], b2[H], W3[K][H], b3[K].
+ * mlp_forward: X [B][F] -> Y [B][K]; work holds 2*B*H floats.
+ * mlp_grad: masked mean squared error against T with mask (mask_sum = its
+ *   sum) and the gradient of every parameter; work holds B*(4H+2K) floats.
+ * mlp_adam: one Adam step (beta 0.9 / 0.999, eps 1e-8) at step >= 1.
+ * All pointers are device pointers; work is queued on `stream`. */
+#define CUFINUFFT_MLP_FEATURES 14
+#define CUFINUFFT_MLP_HIDDEN 32
+#define CUFINUFFT_MLP_CLASSES 9
+#define CUFINUFFT_MLP_PARAMS                                                             \
+  (CUFINUFFT_MLP_HIDDEN * CUFINUFFT_MLP_FEATURES + CUFINUFFT_MLP_HIDDEN +                 \
+   CUFINUFFT_MLP_HIDDEN * CUFINUFFT_MLP_HIDDEN + CUFINUFFT_MLP_HIDDEN +                   \
+   CUFINUFFT_MLP_CLASSES * CUFINUFFT_MLP_HIDDEN + CUFINUFFT_MLP_CLASSES)
+int cufinufft_features(cufinufft_plan plan, float* features);
+int cufinufftf_features(cufinufftf_plan plan, float* features);
+/* Switch a plan with points set to layout class cls (0-8, see autotune). */
+int cufinufft_set_layout_class(cufinufft_plan plan, int cls);
+int cufinufftf_set_layout_class(cufinufftf_plan plan, int cls);
+int cufinufft_mlp_forward(const float* params, const float* X, int B, float* Y, float* work,
+                          cudaStream_t stream);
+int cufinufft_mlp_grad(const float* params, const float* X, const float* T, const float* mask,
+                       int B, float mask_sum, float* grad, float* loss, float* work,
+                       cudaStream_t stream);
+int cufinufft_mlp_adam(float* params, const float* grad, float* m, float* v, int step, float lr,
+                       cudaStream_t stream);
+
+/* Batches (no counterpart in the reference): many plans of one type,
+ * dimension, precision and kernel width -- different N, M and ntransf --
+ * executed together.  batch_make takes plans whose points are set (they must
+ * outlive the batch and keep their points); batch_execute takes host arrays
+ * of nplans device pointers (c[i], fk[i] as for plan i's execute) and runs
+ * every plan's whole ntransf at once: multi-plan spread/interp and
+ * deconvolve/amplify kernels plus one cuFFT call per plan, captured once as a
+ * CUDA graph and replayed.  Results are ordered before later work on the
+ * legacy default stream. */
+typedef struct cufinufft_batch_s* cufinufft_batch;
+typedef struct cufinufftf_batch_s* cufinufftf_batch;
+int cufinufft_batch_make(int nplans, cufinufft_plan* plans, cufinufft_batch* batch);
+int cufinufftf_batch_make(int nplans, cufinufftf_plan* plans, cufinufftf_batch* batch);
+int cufinufft_batch_execute(cufinufft_batch batch, cuDoubleComplex** c, cuDoubleComplex** fk);
+int cufinufftf_batch_execute(cufinufftf_batch batch, cuFloatComplex** c, cuFloatComplex** fk);
+int cufinufft_batch_destroy(cufinufft_batch batch);
+int cufinufftf_batch_destroy(cufinufftf_batch batch);
+
 /* Allocation-free spreading; it has no counterpart in the reference.  For
  * callers that cannot allocate device memory at the point of use (code inside
  * a framework that owns all device memory, real-time loops, memory-budgeted

@@ -162,3 +162,54 @@ def test_library_chosen_method(single, ntype, dim):
     tol = 1e-5 if single else 1e-9
     info = _case(ntype, dim, 0, 1, single, 0, tol, seed=31)
     assert info["method"] in (1, 2)
+
+
+@pytest.mark.parametrize("single", [True, False], ids=["f32", "f64"])
+@pytest.mark.parametrize("ntype", [1, 2])
+@pytest.mark.parametrize("dim", [1, 2, 3])
+def test_set_layout_and_autotune_keep_results(single, ntype, dim):
+    """Re-sorting the stored points for another method / bin size (and the
+    autotuner, which does that for each candidate) leaves the results equal
+    to the oracle's."""
+    import torch
+
+    from cufinufft_gb300 import cufinufft
+    rng = np.random.default_rng(40 + dim + 3 * ntype)
+    tol = 1e-5 if single else 1e-9
+    dt = np.float32 if single else np.float64
+    modes = MODES[dim]
+    M = 2500
+    pts = NC.points(rng, dim, M, dtype=dt, edges=False)
+    data = NC.strengths(rng, M) if ntype == 1 else NC.coeffs(rng, modes)
+    data = data.astype(np.complex64 if single else np.complex128)
+    ref = NC.oracle_nufft(ntype, modes, [p.astype(np.float64) for p in pts],
+                          data.astype(np.complex128), tol, single)
+    plan = cufinufft(ntype, modes[::-1], eps=tol, dtype=dt)
+    plan.set_pts(*[torch.from_numpy(p).cuda() for p in pts[::-1]])
+    d = torch.from_numpy(data).cuda()
+
+    def run():
+        if ntype == 1:
+            out = torch.zeros((1,) + modes[::-1], dtype=d.dtype, device="cuda")
+            plan.execute(d, out)
+        else:
+            out = torch.zeros((1, M), dtype=d.dtype, device="cuda")
+            plan.execute(out, d)
+        torch.cuda.synchronize()
+        o = out.cpu().numpy()
+        return float(np.linalg.norm(o.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel()))
+
+    bound = 2e-5 if single else 1e-10
+    assert run() < bound
+    layouts = [(1, (7,) * dim), (2, (9,) * dim)] if not (ntype == 2 and dim == 1) else [(1, (7,))]
+    for method, bins in layouts:
+        plan.set_layout(method, bins, maxsubprobsize=100)
+        info = plan.info()
+        assert info["method"] == method and info["binsizex"] == bins[0]
+        assert run() < bound
+    entries = plan.autotune()
+    tried = [e for e in entries[1:] if e["ms"] >= 0]
+    assert tried and entries[0]["ms"] == min(e["ms"] for e in tried)
+    info = plan.info()
+    assert info["method"] == entries[0]["method"] and info["binsizex"] == entries[0]["binsizex"]
+    assert run() < bound
