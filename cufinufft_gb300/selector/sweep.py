@@ -31,10 +31,15 @@ def run(n: int, out: str, start: int = 0, device: int = 0, log_every: int = 50,
         s = W.spec(i)
         dt = np.float32 if s["single"] else np.float64
         pts = W.points(s, dev)
-        plan = cufinufft(s["type"], tuple(s["modes"])[::-1], eps=s["tol"], dtype=dt, gpu_method=1)
-        plan.set_pts(*pts[::-1])
-        f = plan.features()
-        entries = plan.autotune()
+        try:
+            plan = cufinufft(s["type"], tuple(s["modes"])[::-1], eps=s["tol"], dtype=dt,
+                             gpu_method=1)
+            plan.set_pts(*pts[::-1])
+            f = plan.features()
+            entries = plan.autotune()
+        except RuntimeError as exc:
+            print(f"workload {i} skipped: {exc}", flush=True)
+            continue
         ms = [e["ms"] for e in entries[1:10]]
         feats.append(list(f))
         times.append(ms)

@@ -83,7 +83,7 @@ def points(s: dict, device):
         pts = []
         for d in range(dim):
             nf = 2 * s["modes"][d]
-            a = float(torch.rand(1, generator=g).item()) * two_pi - math.pi
+            a = float(torch.rand(1, generator=g, device=device).item()) * two_pi - math.pi
             w = two_pi * 8 / nf
             pts.append(torch.remainder(a + w * torch.rand(M, generator=g, device=device,
                                                           dtype=torch.float64) + math.pi, two_pi)

@@ -64,7 +64,7 @@ def adam(p, g, m, v, step, lr, b1=0.9, b2=0.999, eps=1e-8):
 def read_weights_header(path):
     """(trained, mean[F], std[F], params[NPARAM]) from selector_weights.h."""
     text = open(path).read()
-    trained = int(re.search(r"kSelectorTrained\s*=\s*(\d+)", text).group(1))
+    trained = int(re.search(r"constexpr int kSelectorTrained\s*=\s*(\d+);", text).group(1))
 
     def arr(name):
         body = re.search(name + r"\[[^\]]*\]\s*=\s*\{([^}]*)\}", text).group(1)
