@@ -70,7 +70,8 @@ class PlanInfo(ctypes.Structure):
     _fields_ = [(n, c_int) for n in (
         "type", "dim", "ms", "mt", "mu", "nf1", "nf2", "nf3", "ns", "M", "ntransf",
         "maxbatchsize", "method", "sort", "binsizex", "binsizey", "binsizez", "nbins",
-        "nsubprob", "kerevalmeth")] + [("beta", c_double), ("es_c", c_double)]
+        "nsubprob", "kerevalmeth")] + [("beta", c_double), ("es_c", c_double),
+                                       ("line_fft", c_int)]
 
 
 CufinufftPlan = c_void_p

@@ -10,6 +10,7 @@
 #include <cufft.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -93,7 +94,11 @@ template <typename T> static void release(Plan<T>* p) {
   for (int k = 0; k < 3; ++k) {
     cudaFree(p->fac[k]);
     p->fac[k] = nullptr;
+    cudaFree(p->tw[k]);
+    p->tw[k] = nullptr;
+    p->rad[k].clear();
   }
+  p->line_fft = false;
   p->horner.clear();
   cudaFree(p->sel_buf);
   p->sel_buf = nullptr;
@@ -107,6 +112,9 @@ template <typename T> static void release(Plan<T>* p) {
   cudaFree(p->sub_to_bin);
   p->count = p->start = p->sub_start = p->scan_tmp = p->sub_to_bin = nullptr;
   p->cap_sub = 0;
+  cudaFree(p->cls_count);
+  p->cls_count = nullptr;
+  p->cap_cls = 0;
   if (p->h_total) cudaFreeHost(p->h_total);
   p->h_total = nullptr;
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
@@ -125,6 +133,238 @@ static int make_fft(Plan<T>* p, int batch, cufftHandle* h) {
   CFG_CUFFT(cufftPlanMany(h, p->dim, n, n, 1, dist, n, 1, dist, fft_type<T>(), batch));
   CFG_CUFFT(cufftSetStream(*h, p->stream));
   return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Pruned line FFTs (fftpass.cu): with CUFINUFFT_FFT=line, used when every
+// axis length is 2,3,5-smooth and fits one block's shared memory (8192 FP32
+// / 4096 FP64 points); otherwise the whole-grid cuFFT path runs.
+
+// Radices (8, 4, 2, 5, 3) whose product is L; empty if L has another factor.
+static std::vector<int> radix_plan(int L) {
+  std::vector<int> r;
+  if (L < 2) return r;
+  for (int R : {8, 4, 2, 5, 3})
+    while (L % R == 0) {
+      r.push_back(R);
+      L /= R;
+    }
+  if (L != 1) r.clear();
+  return r;
+}
+
+template <typename T>
+static bool use_line_fft(const Plan<T>* p) {
+  const char* v = std::getenv("CUFINUFFT_FFT");
+  if (v == nullptr || std::strcmp(v, "line") != 0) return false;
+  for (int k = 0; k < p->dim; ++k) {
+    const std::vector<int> r = radix_plan(p->nf[k]);
+    if (p->nf[k] > line_fft_cap<T>() || r.empty() || r.size() > 24) return false;
+  }
+  return true;
+}
+
+template <typename T>
+static int make_line_fft(Plan<T>* p) {
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  for (int k = 0; k < p->dim; ++k) {
+    const int L = p->nf[k];
+    p->rad[k] = radix_plan(L);
+    std::vector<cplx_t<T>> h((size_t)L);
+    for (int m = 0; m < L; ++m) {
+      const long double ang = two_pi * (long double)m / (long double)L;
+      h[m].x = (T)(double)cosl(ang);
+      h[m].y = (T)(double)((long double)p->iflag * sinl(ang));
+    }
+    CFG_CUDA(cudaMalloc(&p->tw[k], sizeof(cplx_t<T>) * (size_t)L));
+    CFG_CUDA(cudaMemcpy(p->tw[k], h.data(), sizeof(cplx_t<T>) * (size_t)L, cudaMemcpyHostToDevice));
+  }
+  CFG_CUDA(line_fft_prepare<T>());
+  p->line_fft = true;
+  return 0;
+}
+
+// Lines per block: a power of two with G * L at most half the cap (two
+// padded buffers of ~34 KB, three blocks per SM); longer lines run one per
+// block.
+template <typename T>
+static LineArgs<T> line_base(const Plan<T>* p, int axis, int B, int nlines) {
+  LineArgs<T> a;
+  std::memset(&a, 0, sizeof(a));
+  a.L = p->nf[axis];
+  a.dir = p->iflag;
+  const int cap = line_fft_cap<T>() / 2;
+  int G = 1, lg = 0;
+  while (G < 256 && G < nlines && 2 * G * a.L <= cap) {
+    G *= 2;
+    ++lg;
+  }
+  a.G = G;
+  a.log2G = lg;
+  a.nlines = nlines;
+  a.ntr = B;
+  a.nrad = (int)p->rad[axis].size();
+  for (int s = 0; s < a.nrad; ++s) a.rad[s] = p->rad[axis][s];
+  a.tw = p->tw[axis];
+  return a;
+}
+
+static LineSide line_side(long long st, long long sa, long long sb, long long sp, int pmode, int Np) {
+  LineSide s;
+  std::memset(&s, 0, sizeof(s));
+  s.st = st;
+  s.sa = sa;
+  s.sb = sb;
+  s.sp = sp;
+  s.pmode = pmode;
+  s.Np = Np;
+  return s;
+}
+static void corner_a(LineSide* s, int N, int nf) {
+  s->acorner = 1;
+  s->Na = N;
+  s->nfa = nf;
+}
+static void corner_b(LineSide* s, int N, int nf) {
+  s->bcorner = 1;
+  s->Nb = N;
+  s->nfb = nf;
+}
+
+// The axis passes of one batch of B transforms, in order.  Type 2: modes fk
+// -> grid fw, the first pass fused with the amplification.  Type 1: grid fw
+// -> modes fk, the last pass fused with the deconvolution.
+template <typename T>
+static std::vector<LineArgs<T>> line_passes(const Plan<T>* p, cplx_t<T>* fk, int B) {
+  const long long Nf = grid_cells(p);
+  const long long Nm = (long long)p->N[0] * p->N[1] * p->N[2];
+  const int n0 = p->nf[0], n1 = p->nf[1], n2 = p->nf[2];
+  const int N0 = p->N[0], N1 = p->N[1], N2 = p->N[2];
+  const long long n01 = (long long)n0 * n1, N01 = (long long)N0 * N1;
+  cplx_t<T>* fw = p->fw;
+  std::vector<LineArgs<T>> v;
+  LineArgs<T> a;
+  if (p->type == 2) {
+    if (p->dim == 1) {
+      a = line_base(p, 0, B, 1);
+      a.A = 1;
+      a.in = fk;
+      a.out = fw;
+      a.si = line_side(Nm, 0, 0, 1, 1, N0);
+      a.so = line_side(Nf, 0, 0, 1, 0, 0);
+      a.fp = p->fac[0];
+      v.push_back(a);
+    } else if (p->dim == 2) {
+      a = line_base(p, 1, B, N0);  // y over the mode columns
+      a.A = N0;
+      a.in = fk;
+      a.out = fw;
+      a.si = line_side(Nm, 1, 0, N0, 1, N1);
+      a.so = line_side(Nf, 1, 0, n0, 0, 0);
+      corner_a(&a.so, N0, n0);
+      a.fa = p->fac[0];
+      a.fp = p->fac[1];
+      v.push_back(a);
+      a = line_base(p, 0, B, n1);  // x over every row
+      a.A = n1;
+      a.in = fw;
+      a.out = fw;
+      a.si = line_side(Nf, n0, 0, 1, 2, N0);
+      a.so = line_side(Nf, n0, 0, 1, 0, 0);
+      v.push_back(a);
+    } else {
+      a = line_base(p, 2, B, (int)N01);  // z over the (x, y) mode columns
+      a.A = N0;
+      a.in = fk;
+      a.out = fw;
+      a.si = line_side(Nm, 1, N0, N01, 1, N2);
+      a.so = line_side(Nf, 1, n0, n01, 0, 0);
+      corner_a(&a.so, N0, n0);
+      corner_b(&a.so, N1, n1);
+      a.fa = p->fac[0];
+      a.fb = p->fac[1];
+      a.fp = p->fac[2];
+      v.push_back(a);
+      a = line_base(p, 1, B, N0 * n2);  // y over (x mode column, every z)
+      a.A = N0;
+      a.in = fw;
+      a.out = fw;
+      a.si = line_side(Nf, 1, n01, n0, 2, N1);
+      corner_a(&a.si, N0, n0);
+      a.so = line_side(Nf, 1, n01, n0, 0, 0);
+      corner_a(&a.so, N0, n0);
+      v.push_back(a);
+      a = line_base(p, 0, B, n1 * n2);  // x over every (y, z) row
+      a.A = n1;
+      a.in = fw;
+      a.out = fw;
+      a.si = line_side(Nf, n0, n01, 1, 2, N0);
+      a.so = line_side(Nf, n0, n01, 1, 0, 0);
+      v.push_back(a);
+    }
+  } else {
+    if (p->dim == 1) {
+      a = line_base(p, 0, B, 1);
+      a.A = 1;
+      a.in = fw;
+      a.out = fk;
+      a.si = line_side(Nf, 0, 0, 1, 0, 0);
+      a.so = line_side(Nm, 0, 0, 1, 1, N0);
+      a.fp = p->fac[0];
+      a.fac_on_out = 1;
+      v.push_back(a);
+    } else if (p->dim == 2) {
+      a = line_base(p, 0, B, n1);  // x over every row, keep the x modes
+      a.A = n1;
+      a.in = fw;
+      a.out = fw;
+      a.si = line_side(Nf, n0, 0, 1, 0, 0);
+      a.so = line_side(Nf, n0, 0, 1, 2, N0);
+      v.push_back(a);
+      a = line_base(p, 1, B, N0);  // y over the x mode columns -> fk
+      a.A = N0;
+      a.in = fw;
+      a.out = fk;
+      a.si = line_side(Nf, 1, 0, n0, 0, 0);
+      corner_a(&a.si, N0, n0);
+      a.so = line_side(Nm, 1, 0, N0, 1, N1);
+      a.fa = p->fac[0];
+      a.fp = p->fac[1];
+      a.fac_on_out = 1;
+      v.push_back(a);
+    } else {
+      a = line_base(p, 0, B, n1 * n2);  // x over every (y, z) row
+      a.A = n1;
+      a.in = fw;
+      a.out = fw;
+      a.si = line_side(Nf, n0, n01, 1, 0, 0);
+      a.so = line_side(Nf, n0, n01, 1, 2, N0);
+      v.push_back(a);
+      a = line_base(p, 1, B, N0 * n2);  // y over (x mode column, every z)
+      a.A = N0;
+      a.in = fw;
+      a.out = fw;
+      a.si = line_side(Nf, 1, n01, n0, 0, 0);
+      corner_a(&a.si, N0, n0);
+      a.so = line_side(Nf, 1, n01, n0, 2, N1);
+      corner_a(&a.so, N0, n0);
+      v.push_back(a);
+      a = line_base(p, 2, B, (int)N01);  // z over the (x, y) mode columns -> fk
+      a.A = N0;
+      a.in = fw;
+      a.out = fk;
+      a.si = line_side(Nf, 1, n0, n01, 0, 0);
+      corner_a(&a.si, N0, n0);
+      corner_b(&a.si, N1, n1);
+      a.so = line_side(Nm, 1, N0, N01, 1, N2);
+      a.fa = p->fac[0];
+      a.fb = p->fac[1];
+      a.fp = p->fac[2];
+      a.fac_on_out = 1;
+      v.push_back(a);
+    }
+  }
+  return v;
 }
 
 template <typename T>
@@ -211,13 +451,19 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   CFG_CUDA(cudaMalloc(&p->sub_start, sizeof(int) * ((size_t)p->nbins + 1)));
   CFG_CUDA(cudaMalloc(&p->scan_tmp, sizeof(int) * (size_t)scan_tmp_ints(p->nbins)));
 
-  int e = make_fft(p, p->maxbatch, &p->fft);
-  if (e) return e;
-  p->have_fft = true;
-  if (p->rem) {
-    e = make_fft(p, p->rem, &p->fft_rem);
+  int e = 0;
+  if (use_line_fft(p)) {
+    e = make_line_fft(p);
     if (e) return e;
-    p->have_fft_rem = true;
+  } else {
+    e = make_fft(p, p->maxbatch, &p->fft);
+    if (e) return e;
+    p->have_fft = true;
+    if (p->rem) {
+      e = make_fft(p, p->rem, &p->fft_rem);
+      if (e) return e;
+      p->have_fft_rem = true;
+    }
   }
 
   FseriesNodes nodes;
@@ -255,6 +501,39 @@ static int ensure_points(Plan<T>* p, int M) {
 template <typename T>
 static int select_layout(Plan<T>* p);
 
+// Bank-class order inside bins for method 2 (BankOrder in kernels.h): the
+// per (bin, class) counters, zeroed on the plan stream.  Plain bin order for
+// method 1, when the counters would exceed 2^24 ints, or with
+// CUFINUFFT_BANK_ORDER=0.
+template <typename T>
+static int bank_order(Plan<T>* p, int method, const int bs[3], int nbins, BankOrder* o) {
+  std::memset(o, 0, sizeof(*o));
+  if (method != 2) return 0;
+  // only the one-thread-per-point tile kernels gain: interpolation by default,
+  // spreading only when forced to that variant (the warp-cooperative spread,
+  // measured on clustered 3D points, is slower with this order)
+  const bool per_point = p->type == 2 ? p->variant != 2 : p->variant == 1;
+  if (!per_point) return 0;
+  if (const char* v = std::getenv("CUFINUFFT_BANK_ORDER"))
+    if (std::strcmp(v, "0") == 0) return 0;  // plain bin order (for comparisons)
+  const int ncls = 128 / (int)sizeof(cplx_t<T>);
+  const size_t n = (size_t)nbins * ncls;
+  if (n > ((size_t)1 << 24)) return 0;
+  if (n > p->cap_cls) {
+    cudaFree(p->cls_count);
+    p->cls_count = nullptr;
+    p->cap_cls = 0;
+    CFG_CUDA(cudaMalloc(&p->cls_count, sizeof(int) * n));
+    p->cap_cls = n;
+  }
+  CFG_CUDA(cudaMemsetAsync(p->cls_count, 0, sizeof(int) * n, p->stream));
+  o->cls_count = p->cls_count;
+  o->ncls = ncls;
+  o->tx = bs[0] + p->sp.ns - 1;
+  o->ty = p->dim > 1 ? bs[1] + p->sp.ns - 1 : 1;
+  return 0;
+}
+
 template <typename T>
 static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
   if (!p->planned) return CUFINUFFT_ERR_GENERIC;
@@ -287,6 +566,8 @@ static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
     CFG_CUDA(launch_place_unsorted<T>(a, p->stream));
   } else {
     CFG_CUDA(cudaMemsetAsync(p->count, 0, sizeof(int) * (size_t)p->nbins, p->stream));
+    e = bank_order(p, p->method, p->bs, p->nbins, &a.bank);
+    if (e) return e;
     CFG_CUDA(launch_bin_count<T>(a, p->stream));
     CFG_CUDA(launch_scan(p->count, p->start, p->nbins, 0, 1, p->scan_tmp, p->stream));
     CFG_CUDA(launch_permute<T>(a, p->stream));
@@ -394,16 +675,33 @@ static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
       CFG_CUDA(cudaMemsetAsync(p->fw, 0, sizeof(cplx_t<T>) * (size_t)Nf * B, p->stream));
       CFG_CUDA(run_spread(p, a));
       mark(p, ev[1]);
-      CFG_CUFFT(fft_exec(h, p->fw, p->iflag));
-      mark(p, ev[2]);
-      CFG_CUDA(launch_deconvolve<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
-                                    p->fac[1], p->fac[2], B, p->stream));
+      if (p->line_fft) {
+        const std::vector<LineArgs<T>> passes = line_passes(p, fk + (size_t)b0 * Nm, B);
+        for (size_t i = 0; i < passes.size(); ++i) {
+          if (i + 1 == passes.size()) mark(p, ev[2]);  // last pass: deconvolution fused
+          CFG_CUDA(launch_line_fft<T>(passes[i], p->stream));
+        }
+      } else {
+        CFG_CUFFT(fft_exec(h, p->fw, p->iflag));
+        mark(p, ev[2]);
+        CFG_CUDA(launch_deconvolve<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
+                                      p->fac[1], p->fac[2], B, p->stream));
+      }
     } else {
-      CFG_CUDA(launch_amplify<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
-                                 p->fac[1], p->fac[2], B, p->stream));
-      mark(p, ev[1]);
-      CFG_CUFFT(fft_exec(h, p->fw, p->iflag));
-      mark(p, ev[2]);
+      if (p->line_fft) {
+        const std::vector<LineArgs<T>> passes = line_passes(p, fk + (size_t)b0 * Nm, B);
+        for (size_t i = 0; i < passes.size(); ++i) {
+          CFG_CUDA(launch_line_fft<T>(passes[i], p->stream));
+          if (i == 0) mark(p, ev[1]);  // first pass: amplification fused
+        }
+        mark(p, ev[2]);
+      } else {
+        CFG_CUDA(launch_amplify<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
+                                   p->fac[1], p->fac[2], B, p->stream));
+        mark(p, ev[1]);
+        CFG_CUFFT(fft_exec(h, p->fw, p->iflag));
+        mark(p, ev[2]);
+      }
       a.fw_in = p->fw;
       a.c_out = c + (size_t)b0 * p->M;
       CFG_CUDA(run_interp(p, a));
@@ -438,6 +736,7 @@ static void fill_info(const Plan<T>* p, cufinufft_plan_info* info) {
   info->kerevalmeth = p->opts.gpu_kerevalmeth;
   info->beta = p->sp.beta;
   info->es_c = p->sp.c;
+  info->line_fft = p->line_fft ? 1 : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -537,6 +836,8 @@ static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub)
     a.count = p->count;
     a.rank = p->rank;
     a.start = p->start;
+    e = bank_order(p, method, bs, (int)nbins, &a.bank);
+    if (e) return e;
     CFG_CUDA(cudaMemsetAsync(p->count, 0, sizeof(int) * (size_t)nbins, p->stream));
     CFG_CUDA(launch_rebin_count<T>(a, p->stream));
     CFG_CUDA(launch_scan(p->count, p->start, (int)nbins, 0, 1, p->scan_tmp, p->stream));

@@ -1,6 +1,8 @@
 // batch.cu -- the batch C ABI: building the descriptor tables, capturing the
 // batch sequence into a CUDA graph and replaying it (kernels in batch.cuh,
 // instantiated per precision in batch_f.cu / batch_d.cu).
+#include <cmath>
+
 #include "batch.cuh"
 
 namespace cfg {
@@ -128,6 +130,8 @@ static int batch_make(Batch<T>* b, int nplans, Plan<T>** plans) {
     D.idx = p->idx;
     D.beta = (T)p->sp.beta;
     D.c = (T)p->sp.c;
+    D.e_beta = (T)std::exp(p->sp.beta);
+    D.bl2e = (T)(p->sp.beta * 1.44269504088896340736);
     D.fw = fw;
     D.task0 = task;
     D.row0 = row;

@@ -34,6 +34,7 @@ template <typename T> struct BatchDesc {
   const int* i0[3];
   const T* d[3];
   T beta, c;
+  T e_beta, bl2e;  // e^beta and beta log2(e) (FP32 kernel evaluation)
   cplx_t<T>* fw;
   const cplx_t<T>* c_in;    // type 1 strengths
   cplx_t<T>* c_out;         // type 2 values
@@ -62,9 +63,11 @@ __device__ __forceinline__ int find_plan(const BatchDesc<T>* D, int nplans, long
 }
 
 template <typename T, int NS>
-__device__ __forceinline__ T batch_tap(T d, int j, T beta, T c) {
+__device__ __forceinline__ T batch_tap(T d, int j, const BatchDesc<T>& P) {
   const T x = d - T(0.5) * T(NS) + T(j);
-  return es_value(c * x * x, beta);
+  const T z = P.c * x * x;
+  if constexpr (sizeof(T) == 4) return es_value_fast(z, P.e_beta, P.bl2e);
+  else return es_value(z, P.beta);
 }
 
 // Spreading, warp-cooperative, NU-point driven (as k_spread_gm_wc), over the
@@ -88,11 +91,11 @@ k_batch_spread(const BatchDesc<T>* D, int nplans, long long ntasks) {
     const bool valid = g < PPW && pl < P.M;
     const int p = valid ? (int)pl : P.M - 1;
     const int xj = wrap_idx(P.i0[0][p] + jj, P.nf[0]);
-    const T kx = batch_tap<T, NS>(P.d[0][p], jj, P.beta, P.c);
+    const T kx = batch_tap<T, NS>(P.d[0][p], jj, P);
     T ky = T(1), kz = T(1);
     int i2 = 0, i3 = 0;
-    if (DIM > 1) { i2 = P.i0[1][p]; ky = batch_tap<T, NS>(P.d[1][p], jj, P.beta, P.c); }
-    if (DIM > 2) { i3 = P.i0[2][p]; kz = batch_tap<T, NS>(P.d[2][p], jj, P.beta, P.c); }
+    if (DIM > 1) { i2 = P.i0[1][p]; ky = batch_tap<T, NS>(P.d[1][p], jj, P); }
+    if (DIM > 2) { i3 = P.i0[2][p]; kz = batch_tap<T, NS>(P.d[2][p], jj, P); }
     const int src = P.idx[p];
     for (int t = 0; t < P.ntr; ++t) {
       const C v = P.c_in[(size_t)t * P.M + src];
@@ -134,11 +137,11 @@ k_batch_interp(const BatchDesc<T>* D, int nplans, long long ntasks) {
     const bool valid = pl < P.M;
     const int p = valid ? (int)pl : P.M - 1;
     const int xj = wrap_idx(P.i0[0][p] + jj, P.nf[0]);
-    const T kx = batch_tap<T, NS>(P.d[0][p], jj, P.beta, P.c);
+    const T kx = batch_tap<T, NS>(P.d[0][p], jj, P);
     T ky = T(1), kz = T(1);
     int i2 = 0, i3 = 0;
-    if (DIM > 1) { i2 = P.i0[1][p]; ky = batch_tap<T, NS>(P.d[1][p], jj, P.beta, P.c); }
-    if (DIM > 2) { i3 = P.i0[2][p]; kz = batch_tap<T, NS>(P.d[2][p], jj, P.beta, P.c); }
+    if (DIM > 1) { i2 = P.i0[1][p]; ky = batch_tap<T, NS>(P.d[1][p], jj, P); }
+    if (DIM > 2) { i3 = P.i0[2][p]; kz = batch_tap<T, NS>(P.d[2][p], jj, P); }
     const int dst = P.idx[p];
     for (int t = 0; t < P.ntr; ++t) {
       const C* gt = P.fw + (size_t)t * P.Nf + xj;
@@ -291,11 +294,11 @@ k_batch_spread_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
       const bool valid = g < PPW && pl < st.np;
       const int p = st.p0 + (valid ? pl : st.np - 1);
       const int lx = P.i0[0][p] - st.ox;
-      const T kx = batch_tap<T, NS>(P.d[0][p], jj, P.beta, P.c);
+      const T kx = batch_tap<T, NS>(P.d[0][p], jj, P);
       T ky = T(1), kz = T(1);
       int ly = 0, lz = 0;
-      if (DIM > 1) { ly = P.i0[1][p] - st.oy; ky = batch_tap<T, NS>(P.d[1][p], jj, P.beta, P.c); }
-      if (DIM > 2) { lz = P.i0[2][p] - st.oz; kz = batch_tap<T, NS>(P.d[2][p], jj, P.beta, P.c); }
+      if (DIM > 1) { ly = P.i0[1][p] - st.oy; ky = batch_tap<T, NS>(P.d[1][p], jj, P); }
+      if (DIM > 2) { lz = P.i0[2][p] - st.oz; kz = batch_tap<T, NS>(P.d[2][p], jj, P); }
       const C v = cin[P.idx[p]];
       const T vr = v.x * kx, vi = v.y * kx;
       const int off0 = (lz * st.TY + ly) * st.TX + lx + jj;
@@ -352,19 +355,19 @@ k_batch_interp_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
       T k1[NS], k2[NS];
       const int lx = P.i0[0][p] - st.ox;
 #pragma unroll
-      for (int j = 0; j < NS; ++j) k1[j] = batch_tap<T, NS>(P.d[0][p], j, P.beta, P.c);
+      for (int j = 0; j < NS; ++j) k1[j] = batch_tap<T, NS>(P.d[0][p], j, P);
       int ly = 0, lz = 0;
       if (DIM > 1) {
         ly = P.i0[1][p] - st.oy;
 #pragma unroll
-        for (int j = 0; j < NS; ++j) k2[j] = batch_tap<T, NS>(P.d[1][p], j, P.beta, P.c);
+        for (int j = 0; j < NS; ++j) k2[j] = batch_tap<T, NS>(P.d[1][p], j, P);
       }
       T d3 = T(0);
       if (DIM > 2) { lz = P.i0[2][p] - st.oz; d3 = P.d[2][p]; }
       T ar = T(0), ai = T(0);
 #pragma unroll 1
       for (int dz = 0; dz < NZ; ++dz) {
-        const T kz = DIM > 2 ? batch_tap<T, NS>(d3, dz, P.beta, P.c) : T(1);
+        const T kz = DIM > 2 ? batch_tap<T, NS>(d3, dz, P) : T(1);
         const C* plane = tile + ((lz + dz) * st.TY + ly) * st.TX + lx;
 #pragma unroll
         for (int dy = 0; dy < NY; ++dy) {

@@ -67,13 +67,48 @@ __device__ __forceinline__ void place_coord(T x, const AxisMap<T>& a, int& i0, T
 // ---- ES kernel values -----------------------------------------------------
 // phi = exp(beta*sqrt(1 - z)) for z = c x^2 < 1, else 0; evaluated without a
 // branch (the square root of a clamped argument, then a select).
-__device__ __forceinline__ float es_value(float z, float beta) {
-  const float e = expf(beta * sqrtf(fmaxf(1.0f - z, 0.0f)));
-  return z < 1.0f ? e : 0.0f;
+//
+// FP32 uses sqrt(1-z) - 1 = -z / (1 + sqrt(1-z)):
+//   phi = e^beta * 2^(-(beta log2 e) z / (1 + sqrt(1 - z))).
+// The exponent is near 0 where phi is large and large only where phi is
+// small, so the PTX approximations of sqrt, 1/x and 2^x (each within a few
+// ulps) keep a few-ulp error relative to the peak everywhere; the direct
+// form expf(beta * sqrtf(1 - z)) loses about beta ulps at the peak to the
+// rounding of its argument.  e_beta = e^beta and bl2e = beta log2 e are
+// rounded once on the host.  FP64 uses the direct form.
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
+__device__ __forceinline__ float rcp_approx(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float ex2_approx(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float es_value_fast(float z, float e_beta, float bl2e) {
+  const float s = sqrt_approx(fmaxf(1.0f - z, 0.0f));
+  const float v = ex2_approx(-bl2e * z * rcp_approx(1.0f + s)) * e_beta;
+  return z < 1.0f ? v : 0.0f;
+}
+
 __device__ __forceinline__ double es_value(double z, double beta) {
   const double e = exp(beta * sqrt(fmax(1.0 - z, 0.0)));
   return z < 1.0 ? e : 0.0;
+}
+
+// The kernel value the spread/interp kernels use.  (Defined after the
+// evaluators it calls: the names in a template are bound where it is
+// defined.)
+template <typename T>
+__device__ __forceinline__ T es_eval(T z, const KernelCoeffs<T>& kc) {
+  if constexpr (sizeof(T) == 4) return es_value_fast(z, kc.e_beta, kc.bl2e);
+  else return es_value(z, kc.beta);
 }
 
 // ker[j] = phi(d - ns/2 + j), j = 0..NS-1, phi(x) = exp(beta*sqrt(1-c x^2))
@@ -97,7 +132,7 @@ __device__ __forceinline__ void kernel_row(T d, const KernelCoeffs<T>& kc, T* ke
 #pragma unroll
     for (int j = 0; j < NS; ++j) {
       const T x = x0 + T(j);
-      ker[j] = es_value(kc.c * x * x, kc.beta);
+      ker[j] = es_eval(kc.c * x * x, kc);
     }
   }
 }
@@ -114,7 +149,7 @@ __device__ __forceinline__ T kernel_tap(T d, int j, const KernelCoeffs<T>& kc) {
     return v;
   }
   const T x = d - T(0.5) * T(NS) + T(j);
-  return es_value(kc.c * x * x, kc.beta);
+  return es_eval(kc.c * x * x, kc);
 }
 
 // ---- atomics ---------------------------------------------------------------

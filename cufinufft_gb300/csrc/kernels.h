@@ -15,6 +15,19 @@ template <typename T, int DIM>
 cudaError_t interp_dim(int method, int ns, const SpreadArgs<T>& a, cudaStream_t s);
 
 // setpts.cu -- bin sort of the nonuniform points.
+// Order inside a bin for the shared-memory (method 2) kernels.  A point's
+// bank class is the tile address of its first tap modulo ncls (16 for FP32
+// complex, 8 for FP64: one 128-byte bank sweep); the sort places a bin's
+// points round-robin over the classes, so any ncls consecutive points of a
+// bin differ in class and a half-warp's tile accesses (first tap + the same
+// offset for every point) fall in distinct banks.  cls_count == nullptr
+// keeps plain bin order.
+struct BankOrder {
+  int* cls_count;   // [nbins * ncls], zeroed before counting
+  int ncls;         // power of two
+  int tx, ty;       // tile row length and rows per plane (bin size + ns - 1)
+};
+
 template <typename T> struct PlaceArgs {
   const T* x[3];           // caller's coordinates (device)
   AxisMap<T> ax[3];
@@ -27,8 +40,9 @@ template <typename T> struct PlaceArgs {
   int* i0[3];
   T* d[3];
   int* count;              // [nbins] (must be zeroed before bin_count)
-  int* rank;               // [M] rank of the point inside its bin
+  int* rank;               // [M] rank of the point inside its bin (or its class)
   const int* start;        // [nbins+1] exclusive scan of count
+  BankOrder bank;
 };
 template <typename T> cudaError_t launch_bin_count(const PlaceArgs<T>& a, cudaStream_t s);
 template <typename T> cudaError_t launch_permute(const PlaceArgs<T>& a, cudaStream_t s);
@@ -49,6 +63,7 @@ template <typename T> struct RebinArgs {
   int* count;      // [nbins], zeroed before rebin_count
   int* rank;       // [M]
   const int* start;
+  BankOrder bank;
 };
 template <typename T> cudaError_t launch_rebin_count(const RebinArgs<T>& a, cudaStream_t s);
 template <typename T> cudaError_t launch_rebin_permute(const RebinArgs<T>& a, cudaStream_t s);
@@ -87,5 +102,44 @@ template <typename T>
 cudaError_t launch_amplify(int dim, const int nf[3], const int N[3], cplx_t<T>* fw,
                            const cplx_t<T>* fk, const T* fac0, const T* fac1, const T* fac2,
                            int ntr, cudaStream_t s);
+
+
+// Pruned line FFTs (fftpass.cu).  A pass transforms nlines lines of length
+// L; line l has indices la = l % A and lb = l / A.  Each side (input, output)
+// maps a line and a position to memory:
+//   line offset = ma * sa + mb * sb, ma = la, or the grid position of mode
+//   index la when acorner is set (mode la - Na/2 at (la - Na/2) mod nfa),
+//   and likewise for b;
+//   pmode 0: all L positions w at w * sp;
+//   pmode 1: the Np modes only, compact: mode index i at i * sp;
+//   pmode 2: the Np modes only, in place in the grid: at w(i) * sp,
+// where mode index i in [0, Np) is FFT index (i - Np/2) mod L.  Positions
+// outside the modes read as zero (input) or are not written (output).
+// Factors fa[la] * fb[lb] * fp[i] multiply on load (fac_on_out = 0) or on
+// store (1); null factors are 1.
+struct LineSide {
+  long long st, sa, sb, sp;
+  int acorner, Na, nfa;
+  int bcorner, Nb, nfb;
+  int pmode, Np;
+};
+
+template <typename T>
+struct LineArgs {
+  int L, dir, G, log2G, A, nlines, ntr, nrad;
+  int rad[24];
+  const cplx_t<T>* tw;  // exp(dir 2 pi i m / L), m = 0..L-1
+  const cplx_t<T>* in;
+  cplx_t<T>* out;
+  LineSide si, so;
+  const T* fa;
+  const T* fb;
+  const T* fp;
+  int fac_on_out;
+};
+
+template <typename T> int line_fft_cap();
+template <typename T> cudaError_t line_fft_prepare();
+template <typename T> cudaError_t launch_line_fft(const LineArgs<T>& a, cudaStream_t s);
 
 }  // namespace cfg

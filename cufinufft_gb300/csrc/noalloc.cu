@@ -217,6 +217,7 @@ extern "C" int cufinufftf_spread2d_noalloc(int M, const float* x, const float* y
   if (M == 0) return 0;
 
   PlaceArgs<float> pa;
+  memset(&pa, 0, sizeof(pa));  // also plain bin order: pa.bank.cls_count = nullptr
   pa.x[0] = x;
   pa.x[1] = y;
   pa.x[2] = nullptr;
@@ -275,6 +276,8 @@ extern "C" int cufinufftf_spread2d_noalloc(int M, const float* x, const float* y
   a.bins.maxsub = kNaMaxSub;
   a.kc.beta = (float)sp.beta;
   a.kc.c = (float)sp.c;
+  a.kc.e_beta = (float)std::exp(sp.beta);
+  a.kc.bl2e = (float)(sp.beta * 1.44269504088896340736);
   a.kc.horner = 0;
   a.kc.coef_g = nullptr;
   a.g.nf[0] = nf1;

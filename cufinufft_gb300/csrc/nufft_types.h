@@ -40,6 +40,7 @@ constexpr int kMaxHornerRows = kMaxNS + 4;  // degree <= ns + 3
 // constant bank.
 template <typename T> struct KernelCoeffs {
   T beta, c;
+  T e_beta, bl2e;                    // e^beta and beta log2(e) (FP32 kernel evaluation)
   int horner;
   const T* coef_g;                   // device copy, read by kernel_tap (runtime tap index)
   T coef[kMaxHornerRows * kMaxNS];

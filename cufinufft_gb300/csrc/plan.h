@@ -4,6 +4,7 @@
 
 #include <cufft.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -35,6 +36,11 @@ template <typename T> struct Plan {
   cudaStream_t own = nullptr, stream = nullptr;
   cufftHandle fft = 0, fft_rem = 0;
   bool have_fft = false, have_fft_rem = false;
+  // pruned line FFTs (fftpass.cu) instead of cuFFT: per-axis twiddle tables
+  // exp(iflag 2 pi i m / nf_d) and radix sequences
+  bool line_fft = false;
+  C* tw[3] = {nullptr, nullptr, nullptr};
+  std::vector<int> rad[3];
   int rem = 0;
   C* fw = nullptr;
   T* fac[3] = {nullptr, nullptr, nullptr};
@@ -52,6 +58,8 @@ template <typename T> struct Plan {
   int* scan_tmp = nullptr;
   int* sub_to_bin = nullptr;
   size_t cap_sub = 0;
+  int* cls_count = nullptr;  // per (bin, bank class) counts for method 2 ordering
+  size_t cap_cls = 0;
   int* h_total = nullptr;  // pinned readback of the subproblem count
   // stage timing (extension): events recorded around each stage of execute
   bool timing = false;
@@ -146,6 +154,8 @@ inline SpreadArgs<T> spread_args(Plan<T>* p) {
   a.bins.maxsub = p->opts.gpu_maxsubprobsize;
   a.kc.beta = (T)p->sp.beta;
   a.kc.c = (T)p->sp.c;
+  a.kc.e_beta = (T)std::exp(p->sp.beta);
+  a.kc.bl2e = (T)(p->sp.beta * 1.44269504088896340736);
   a.kc.horner = p->horner.empty() ? 0 : 1;
   a.kc.coef_g = p->horner_d;
   for (size_t k = 0; k < p->horner.size() && k < (size_t)(kMaxHornerRows * kMaxNS); ++k)

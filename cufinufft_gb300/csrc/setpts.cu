@@ -34,9 +34,39 @@ __device__ __forceinline__ int point_bin(const PlaceArgs<T>& a, int i, int i0[3]
   return b;
 }
 
+// Bank class of a point whose first taps are i0 (see BankOrder).
+__device__ __forceinline__ int bank_class(const BankOrder& o, const int* bs, int dim, const int i0[3]) {
+  const int lx = i0[0] % bs[0];
+  const int ly = dim > 1 ? i0[1] % bs[1] : 0;
+  const int lz = dim > 2 ? i0[2] % bs[2] : 0;
+  return (lx + o.tx * (ly + o.ty * lz)) & (o.ncls - 1);
+}
+
+// Warp-aggregated rank: one atomic per distinct key in the warp.
+__device__ __forceinline__ int agg_rank(unsigned act, int key, int* counter) {
+  const int lane = threadIdx.x & 31;
+  const unsigned peers = __match_any_sync(act, key);
+  const int leader = __ffs(peers) - 1;
+  int first = 0;
+  if (lane == leader) first = atomicAdd(counter, __popc(peers));
+  first = __shfl_sync(peers, first, leader);
+  return first + __popc(peers & ((1u << lane) - 1u));
+}
+
+// Position inside its bin of the point ranked r in class c: round-robin over
+// the classes, rounds shrinking as classes run out.
+__device__ __forceinline__ int interleave_pos(const BankOrder& o, int b, int c, int r) {
+  const int* cnt = o.cls_count + (long long)b * o.ncls;
+  int pos = 0;
+  for (int k = 0; k < o.ncls; ++k) {
+    const int n = __ldg(cnt + k);
+    pos += min(n, r) + ((k < c && n > r) ? 1 : 0);
+  }
+  return pos;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kPlaceThreads) k_bin_count(PlaceArgs<T> a) {
-  const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
   // warp-uniform trip count so the warp stays converged for __match_any_sync
   for (long long base = (long long)blockIdx.x * blockDim.x; base < a.M; base += stride) {
@@ -48,12 +78,13 @@ __global__ void __launch_bounds__(kPlaceThreads) k_bin_count(PlaceArgs<T> a) {
     int i0[3];
     T d[3];
     const int b = point_bin(a, i, i0, d);
-    const unsigned peers = __match_any_sync(act, b);
-    const int leader = __ffs(peers) - 1;
-    int first = 0;
-    if (lane == leader) first = atomicAdd(&a.count[b], __popc(peers));
-    first = __shfl_sync(peers, first, leader);
-    a.rank[i] = first + __popc(peers & ((1u << lane) - 1u));
+    const int r = agg_rank(act, b, &a.count[b]);
+    if (a.bank.cls_count) {
+      const int key = b * a.bank.ncls + bank_class(a.bank, a.bs, a.dim, i0);
+      a.rank[i] = agg_rank(act, key, a.bank.cls_count + key);
+    } else {
+      a.rank[i] = r;
+    }
   }
 }
 
@@ -63,7 +94,9 @@ __global__ void __launch_bounds__(kPlaceThreads) k_permute(PlaceArgs<T> a) {
     int i0[3];
     T d[3];
     const int b = point_bin(a, i, i0, d);
-    const int pos = a.start[b] + a.rank[i];
+    const int pos = a.start[b] + (a.bank.cls_count
+                                      ? interleave_pos(a.bank, b, bank_class(a.bank, a.bs, a.dim, i0), a.rank[i])
+                                      : a.rank[i]);
     a.idx[pos] = i;
     for (int k = 0; k < 3; ++k) {
       if (k < a.dim) {
@@ -137,7 +170,6 @@ __device__ __forceinline__ int stored_bin(const RebinArgs<T>& a, int i) {
 
 template <typename T>
 __global__ void __launch_bounds__(kPlaceThreads) k_rebin_count(RebinArgs<T> a) {
-  const int lane = threadIdx.x & 31;
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long base = (long long)blockIdx.x * blockDim.x; base < a.M; base += stride) {
     const long long ii = base + threadIdx.x;
@@ -146,19 +178,27 @@ __global__ void __launch_bounds__(kPlaceThreads) k_rebin_count(RebinArgs<T> a) {
     if (!active) continue;
     const int i = (int)ii;
     const int b = stored_bin(a, i);
-    const unsigned peers = __match_any_sync(act, b);
-    const int leader = __ffs(peers) - 1;
-    int first = 0;
-    if (lane == leader) first = atomicAdd(&a.count[b], __popc(peers));
-    first = __shfl_sync(peers, first, leader);
-    a.rank[i] = first + __popc(peers & ((1u << lane) - 1u));
+    const int r = agg_rank(act, b, &a.count[b]);
+    if (a.bank.cls_count) {
+      const int i0[3] = {a.src_i0[0][i], a.dim > 1 ? a.src_i0[1][i] : 0, a.dim > 2 ? a.src_i0[2][i] : 0};
+      const int key = b * a.bank.ncls + bank_class(a.bank, a.bs, a.dim, i0);
+      a.rank[i] = agg_rank(act, key, a.bank.cls_count + key);
+    } else {
+      a.rank[i] = r;
+    }
   }
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kPlaceThreads) k_rebin_permute(RebinArgs<T> a) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += gridDim.x * blockDim.x) {
-    const int pos = a.start[stored_bin(a, i)] + a.rank[i];
+    const int b = stored_bin(a, i);
+    int pos = a.rank[i];
+    if (a.bank.cls_count) {
+      const int i0[3] = {a.src_i0[0][i], a.dim > 1 ? a.src_i0[1][i] : 0, a.dim > 2 ? a.src_i0[2][i] : 0};
+      pos = interleave_pos(a.bank, b, bank_class(a.bank, a.bs, a.dim, i0), pos);
+    }
+    pos += a.start[b];
     a.idx[pos] = a.src_idx[i];
     for (int k = 0; k < 3; ++k) {
       if (k < a.dim) {

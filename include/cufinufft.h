@@ -104,6 +104,7 @@ typedef struct cufinufft_plan_info {
   int type, dim, ms, mt, mu, nf1, nf2, nf3, ns, M, ntransf, maxbatchsize;
   int method, sort, binsizex, binsizey, binsizez, nbins, nsubprob, kerevalmeth;
   double beta, es_c;
+  int line_fft; /* 1: pruned line FFTs (fftpass.cu), 0: cuFFT over the whole grid */
 } cufinufft_plan_info;
 int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info);
 int cufinufftf_get_info(cufinufftf_plan plan, cufinufft_plan_info* info);
