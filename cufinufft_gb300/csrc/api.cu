@@ -187,12 +187,37 @@ static int make_line_fft(Plan<T>* p) {
 // Lines per block: a power of two with G * L at most half the cap (two
 // padded buffers of ~34 KB, three blocks per SM); longer lines run one per
 // block.
+//
+// Power-of-two lines of at least 16 points take the register-resident kernel:
+// block = G * L / 16 threads, G * L <= 4096 FP32 / 2048 FP64 points.  Along
+// x (contiguous lines) G is lowered (down to 64 threads) while that leaves
+// fewer than ~6 blocks per SM.  Along y and z a block's G lines are G
+// adjacent elements of each grid row it reads, so G is never lowered, and
+// lines longer than 1024 FP32 / 512 FP64 points may take twice the points
+// (G = 4 / 2: 32-byte row segments).
 template <typename T>
 static LineArgs<T> line_base(const Plan<T>* p, int axis, int B, int nlines) {
   LineArgs<T> a;
   std::memset(&a, 0, sizeof(a));
   a.L = p->nf[axis];
   a.dir = p->iflag;
+  const int base_elems = line_fft_p2_elems<T>();
+  const int p2_elems = (axis > 0 && a.L > base_elems / 4) ? 2 * base_elems : base_elems;
+  if (a.L >= 16 && (a.L & (a.L - 1)) == 0 && a.L <= p2_elems) {
+    int G = p2_elems / a.L;
+    const long long want = 152LL * 6;
+    while (axis == 0 && G > 1 && G * a.L / 16 > 64 && (long long)((nlines + G - 1) / G) * B < want)
+      G /= 2;
+    int lg = 0;
+    while ((1 << lg) < G) ++lg;
+    a.p2 = 1;
+    a.G = G;
+    a.log2G = lg;
+    a.nlines = nlines;
+    a.ntr = B;
+    a.tw = p->tw[axis];
+    return a;
+  }
   const int cap = line_fft_cap<T>() / 2;
   int G = 1, lg = 0;
   while (G < 256 && G < nlines && 2 * G * a.L <= cap) {

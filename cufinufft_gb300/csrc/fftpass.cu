@@ -157,6 +157,43 @@ template <typename T> struct Dft<T, 5> {
   }
 };
 
+// 16-point DFT as 4 x 4: DFT-4 over n2 (stride 4), twiddles W16^(n1 k2),
+// DFT-4 over n1; X[k2 + 4 k1].
+template <typename T> struct Dft<T, 16> {
+  static __device__ __forceinline__ void run(cplx_t<T>* v, T dir) {
+    using C = cplx_t<T>;
+    const T c1 = T(0.92387953251128675613);  // cos(pi/8)
+    const T s1 = T(0.38268343236508977173);  // sin(pi/8)
+    const T h = T(0.70710678118654752440);   // 1/sqrt(2)
+    C y[4][4];
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) {
+      C a[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
+      Dft<T, 4>::run(a, dir);
+#pragma unroll
+      for (int k2 = 0; k2 < 4; ++k2) y[n1][k2] = a[k2];
+    }
+    const C w1 = C{c1, dir * s1}, w2 = C{h, dir * h}, w3 = C{s1, dir * c1};
+    const C w6 = C{-h, dir * h}, w9 = C{-c1, -dir * s1};
+    y[1][1] = cmul(y[1][1], w1);
+    y[1][2] = cmul(y[1][2], w2);
+    y[1][3] = cmul(y[1][3], w3);
+    y[2][1] = cmul(y[2][1], w2);
+    y[2][2] = cmul_i(y[2][2], dir);
+    y[2][3] = cmul(y[2][3], w6);
+    y[3][1] = cmul(y[3][1], w3);
+    y[3][2] = cmul(y[3][2], w6);
+    y[3][3] = cmul(y[3][3], w9);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) {
+      C b[4] = {y[0][k2], y[1][k2], y[2][k2], y[3][k2]};
+      Dft<T, 4>::run(b, dir);
+#pragma unroll
+      for (int k1 = 0; k1 < 4; ++k1) v[k2 + 4 * k1] = b[k1];
+    }
+  }
+};
+
 // Shared-memory layout of a line: element i at i + i/16.  The extra slot
 // every 16 elements (128 bytes of FP32 complex) spreads the strided Stockham
 // writes (stride R Ns) over the banks instead of piling them onto one.
@@ -358,22 +395,266 @@ k_line_fft(LineArgs<T> a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Power-of-two lines, register-resident passes.  Block = G * L / 16 threads
+// (G lines of L = 2^m >= 16 points, at most 512 threads); radices 16, ...,
+// 16 then one of 8/4/2.
+// Every pass gives each thread exactly 16/R butterflies, so values stay in
+// registers: the first pass loads its 16 inputs straight from global memory
+// (the padding positions of a pruned line are not read), middle passes
+// exchange through one padded shared buffer, and the last pass stores its
+// outputs straight to global memory (only the mode positions of a pruned
+// line), with the per-mode factors applied on the way in or out.
+
+// v[r] *= w^(r * e), r = 1..R-1, from the table entries w^e, w^2e, w^4e,
+// w^8e and products of at most three of them.
+template <typename T, int R>
+__device__ __forceinline__ void twiddle_p2(cplx_t<T>* v, int e, const cplx_t<T>* __restrict__ tw) {
+  using C = cplx_t<T>;
+  const C w1 = __ldg(tw + e);
+  if (R == 2) {
+    v[1] = cmul(v[1], w1);
+    return;
+  }
+  const C w2 = __ldg(tw + 2 * e);
+  const C w3 = cmul(w1, w2);
+  v[1] = cmul(v[1], w1);
+  v[2] = cmul(v[2], w2);
+  v[3] = cmul(v[3], w3);
+  if (R == 4) return;
+  const C w4 = __ldg(tw + 4 * e);
+  v[4] = cmul(v[4], w4);
+  v[5] = cmul(v[5], cmul(w1, w4));
+  v[6] = cmul(v[6], cmul(w2, w4));
+  const C w7 = cmul(w3, w4);
+  v[7] = cmul(v[7], w7);
+  if (R == 8) return;
+  const C w8 = __ldg(tw + 8 * e);
+  v[8] = cmul(v[8], w8);
+  v[9] = cmul(v[9], cmul(w1, w8));
+  v[10] = cmul(v[10], cmul(w2, w8));
+  v[11] = cmul(v[11], cmul(w3, w8));
+  v[12] = cmul(v[12], cmul(w4, w8));
+  v[13] = cmul(v[13], cmul(cmul(w1, w4), w8));
+  v[14] = cmul(v[14], cmul(cmul(w2, w4), w8));
+  v[15] = cmul(v[15], cmul(w7, w8));
+}
+
+// Per-block state of the power-of-two kernel.
+template <typename T> struct P2Ctx {
+  const LineArgs<T>* a;
+  const cplx_t<T>* in;
+  cplx_t<T>* out;
+  cplx_t<T>* buf;
+  int L, lgL, Lp, lgG, T_, line0;
+  T dir;
+};
+
+// Line g and position j of butterfly u: lines contiguous in memory (column
+// passes) take consecutive lanes; otherwise positions do.
+__device__ __forceinline__ void p2_split(int u, int lg_nbf, int lgG, bool lines_fast, int& g, int& j) {
+  if (lines_fast) {
+    g = u & ((1 << lgG) - 1);
+    j = u >> lgG;
+  } else {
+    g = u >> lg_nbf;
+    j = u & ((1 << lg_nbf) - 1);
+  }
+}
+
+// Pass 1 (radix 16, Ns = 1): global -> registers -> DFT -> shared, or
+// global when it is also the last pass (L = 16).
+template <typename T, bool LAST>
+__device__ __forceinline__ void p2_first(const P2Ctx<T>& c) {
+  using C = cplx_t<T>;
+  const LineArgs<T>& a = *c.a;
+  const LineSide& si = a.si;
+  const int lg_nbf = c.lgL - 4;
+  const int nbf = 1 << lg_nbf;
+  int g, j;
+  p2_split(threadIdx.x, lg_nbf, c.lgG, si.sp != 1, g, j);
+  const int line = c.line0 + g;
+  C v[16];
+  if (line < a.nlines) {
+    const int la = line % a.A, lb = line / a.A;
+    const C* src = c.in + side_line(si, la, lb);
+    const bool fac = !a.fac_on_out && (a.fa || a.fb || a.fp);
+    const T f0 = fac ? line_factor(a, la, lb, -1) : T(1);
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+      const int w = j + r * nbf;
+      const int i = si.pmode ? mode_index(w, c.L, si.Np) : -1;
+      if (!si.pmode || i >= 0) {
+        v[r] = src[(long long)(si.pmode == 1 ? i : w) * si.sp];
+        if (fac) v[r] = cscale(v[r], (a.fp && i >= 0) ? f0 * a.fp[i] : f0);
+      } else {
+        v[r] = C{T(0), T(0)};
+      }
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = C{T(0), T(0)};
+  }
+  Dft<T, 16>::run(v, c.dir);
+  if (LAST) {
+    if (line >= a.nlines) return;
+    const LineSide& so = a.so;
+    const int la = line % a.A, lb = line / a.A;
+    C* dst = c.out + side_line(so, la, lb);
+    const bool fac = a.fac_on_out != 0;
+    const T f0 = fac ? line_factor(a, la, lb, -1) : T(1);
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {  // j = 0: output r at position r
+      const int q = so.pmode ? mode_index(r, c.L, so.Np) : r;
+      if (q < 0) continue;
+      C o = v[r];
+      if (fac) o = cscale(o, (a.fp && so.pmode) ? f0 * a.fp[q] : f0);
+      dst[(long long)(so.pmode == 1 ? q : r) * so.sp] = o;
+    }
+  } else {
+    C* l = c.buf + g * c.Lp;
+    const int base = sidx(j * 16);  // j*16 + r stays inside one 16-block
+#pragma unroll
+    for (int r = 0; r < 16; ++r) l[base + r] = v[r];
+  }
+}
+
+// A middle or last pass of radix R with Ns = 2^lgNs: shared -> registers ->
+// twiddle, DFT -> shared (middle) or global (last).
+template <typename T, int R, bool LAST>
+__device__ __forceinline__ void p2_pass(const P2Ctx<T>& c, int lgNs) {
+  using C = cplx_t<T>;
+  constexpr int NB = 16 / R;
+  constexpr int lgR = R == 16 ? 4 : (R == 8 ? 3 : (R == 4 ? 2 : 1));
+  const int lg_nbf = c.lgL - lgR;
+  const int nbf = 1 << lg_nbf;
+  const int Ns = 1 << lgNs;
+  const int lg_tstep = c.lgL - lgNs - lgR;
+  const LineArgs<T>& a = *c.a;
+  const bool lines_fast = LAST && a.so.sp != 1;
+  C v[NB][R];
+  int gg[NB], jj[NB];
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    p2_split(threadIdx.x + b * c.T_, lg_nbf, c.lgG, lines_fast, gg[b], jj[b]);
+    const C* l = c.buf + gg[b] * c.Lp;
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[b][r] = l[sidx(jj[b] + r * nbf)];
+  }
+  __syncthreads();  // every read of this pass is done before any write
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const int k = jj[b] & (Ns - 1);
+    twiddle_p2<T, R>(v[b], k << lg_tstep, a.tw);
+    Dft<T, R>::run(v[b], c.dir);
+  }
+  if (!LAST) {
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const int k = jj[b] & (Ns - 1), q = jj[b] >> lgNs;
+      C* l = c.buf + gg[b] * c.Lp;
+      const int base = (q << (lgNs + lgR)) + k;
+#pragma unroll
+      for (int r = 0; r < R; ++r) l[sidx(base + r * Ns)] = v[b][r];
+    }
+    __syncthreads();
+    return;
+  }
+  // last pass: nbf = Ns, so q = 0 and output r of butterfly j is at j + r Ns
+  const LineSide& so = a.so;
+  const bool fac = a.fac_on_out != 0;
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const int line = c.line0 + gg[b];
+    if (line >= a.nlines) continue;
+    const int la = line % a.A, lb = line / a.A;
+    C* dst = c.out + side_line(so, la, lb);
+    const T f0 = fac ? line_factor(a, la, lb, -1) : T(1);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int w = jj[b] + r * Ns;
+      const int q = so.pmode ? mode_index(w, c.L, so.Np) : w;
+      if (q < 0) continue;
+      C o = v[b][r];
+      if (fac) o = cscale(o, (a.fp && so.pmode) ? f0 * a.fp[q] : f0);
+      dst[(long long)(so.pmode == 1 ? q : w) * so.sp] = o;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512)
+k_line_fft_p2(LineArgs<T> a) {
+  using C = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  P2Ctx<T> c;
+  c.a = &a;
+  c.L = a.L;
+  c.lgL = __ffs(a.L) - 1;
+  c.Lp = a.L + (a.L >> 4) + 1;
+  c.lgG = a.log2G;
+  c.T_ = blockDim.x;
+  c.line0 = blockIdx.x * a.G;
+  c.dir = T(a.dir);
+  c.buf = reinterpret_cast<C*>(smem_raw);
+  // radices: 16 (n16 times), then rem in {1 (none), 2, 4, 8}
+  const int n16 = c.lgL / 4;
+  const int rem = 1 << (c.lgL - 4 * n16);
+  for (int t = blockIdx.y; t < a.ntr; t += gridDim.y) {
+    c.in = a.in + (long long)t * a.si.st;
+    c.out = a.out + (long long)t * a.so.st;
+    if (n16 == 1 && rem == 1) {
+      p2_first<T, true>(c);
+      continue;
+    }
+    p2_first<T, false>(c);
+    __syncthreads();
+    int lgNs = 4;
+    for (int s = 1; s < n16; ++s) {
+      if (s == n16 - 1 && rem == 1) p2_pass<T, 16, true>(c, lgNs);
+      else p2_pass<T, 16, false>(c, lgNs);
+      lgNs += 4;
+    }
+    if (rem == 8) p2_pass<T, 8, true>(c, lgNs);
+    else if (rem == 4) p2_pass<T, 4, true>(c, lgNs);
+    else if (rem == 2) p2_pass<T, 2, true>(c, lgNs);
+    __syncthreads();  // the buffer is reused by the next transform
+  }
+}
+
+// Longest line: 8192 points FP32, 4096 FP64 (two padded buffers of ~68 KB)
+// for the generic kernel.
 template <typename T> constexpr int line_cap() { return sizeof(T) == 4 ? 8192 : 4096; }
+// Power-of-two kernel: G * L <= 4096 FP32 / 2048 FP64 points per block
+// along x (256 / 128 threads, 16 values each), twice that along y and z.
+template <typename T> constexpr int line_p2_elems() { return sizeof(T) == 4 ? 4096 : 2048; }
 
 }  // namespace
 
 template <typename T> int line_fft_cap() { return line_cap<T>(); }
+template <typename T> int line_fft_p2_elems() { return line_p2_elems<T>(); }
 
 template <typename T>
 cudaError_t line_fft_prepare() {
-  return cudaFuncSetAttribute(k_line_fft<T, line_cap<T>()>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              2 * (line_cap<T>() + line_cap<T>() / 16 + 1) * (int)sizeof(cplx_t<T>));
+  cudaError_t e = cudaFuncSetAttribute(k_line_fft<T, line_cap<T>()>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       2 * (line_cap<T>() + line_cap<T>() / 16 + 1) * (int)sizeof(cplx_t<T>));
+  if (e != cudaSuccess) return e;
+  // G * (L + L/16 + 1) <= E * 18/16 for E = G * L <= twice line_p2_elems, L >= 16
+  return cudaFuncSetAttribute(k_line_fft_p2<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              2 * line_p2_elems<T>() * 18 / 16 * (int)sizeof(cplx_t<T>));
 }
 
 template <typename T>
 cudaError_t launch_line_fft(const LineArgs<T>& a, cudaStream_t s) {
   if (a.nlines <= 0 || a.ntr <= 0) return cudaSuccess;
+  if (a.p2) {
+    const int threads = a.G * a.L / 16;
+    const size_t smem = (size_t)a.G * (a.L + a.L / 16 + 1) * sizeof(cplx_t<T>);
+    dim3 grid((a.nlines + a.G - 1) / a.G, a.ntr < 65535 ? a.ntr : 65535);
+    k_line_fft_p2<T><<<grid, threads, smem, s>>>(a);
+    return cudaGetLastError();
+  }
   const size_t smem = 2 * (size_t)a.G * (a.L + a.L / 16 + 1) * sizeof(cplx_t<T>);
   dim3 grid((a.nlines + a.G - 1) / a.G, a.ntr < 65535 ? a.ntr : 65535);
   k_line_fft<T, line_cap<T>()><<<grid, kLineThreads, smem, s>>>(a);
@@ -382,6 +663,8 @@ cudaError_t launch_line_fft(const LineArgs<T>& a, cudaStream_t s) {
 
 template int line_fft_cap<float>();
 template int line_fft_cap<double>();
+template int line_fft_p2_elems<float>();
+template int line_fft_p2_elems<double>();
 template cudaError_t line_fft_prepare<float>();
 template cudaError_t line_fft_prepare<double>();
 template cudaError_t launch_line_fft<float>(const LineArgs<float>&, cudaStream_t);

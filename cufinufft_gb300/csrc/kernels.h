@@ -127,6 +127,7 @@ struct LineSide {
 template <typename T>
 struct LineArgs {
   int L, dir, G, log2G, A, nlines, ntr, nrad;
+  int p2;               // power-of-two kernel (block = G * L / 16 threads)
   int rad[24];
   const cplx_t<T>* tw;  // exp(dir 2 pi i m / L), m = 0..L-1
   const cplx_t<T>* in;
@@ -139,6 +140,7 @@ struct LineArgs {
 };
 
 template <typename T> int line_fft_cap();
+template <typename T> int line_fft_p2_elems();
 template <typename T> cudaError_t line_fft_prepare();
 template <typename T> cudaError_t launch_line_fft(const LineArgs<T>& a, cudaStream_t s);
 
