@@ -71,7 +71,7 @@ class PlanInfo(ctypes.Structure):
         "type", "dim", "ms", "mt", "mu", "nf1", "nf2", "nf3", "ns", "M", "ntransf",
         "maxbatchsize", "method", "sort", "binsizex", "binsizey", "binsizez", "nbins",
         "nsubprob", "kerevalmeth")] + [("beta", c_double), ("es_c", c_double),
-                                       ("line_fft", c_int)]
+                                       ("line_fft", c_int), ("cell_order", c_int)]
 
 
 CufinufftPlan = c_void_p
@@ -187,7 +187,7 @@ _autotune = lib.cufinufft_autotune
 _autotunef = lib.cufinufftf_autotune
 
 # Learned layout selector: plan features, layout classes and the MLP kernels.
-MLP_FEATURES, MLP_HIDDEN, MLP_CLASSES = 14, 32, 9
+MLP_FEATURES, MLP_HIDDEN, MLP_CLASSES = 14, 32, 12
 MLP_PARAMS = (MLP_HIDDEN * MLP_FEATURES + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN
               + MLP_CLASSES * MLP_HIDDEN + MLP_CLASSES)
 for _name in ("cufinufft_features", "cufinufftf_features"):

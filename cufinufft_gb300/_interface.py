@@ -208,8 +208,9 @@ class cufinufft:
         return {"spreadinterp": ms[0], "fft": ms[1], "deconv": ms[2], "batches": nb.value}
 
     def set_layout(self, method, binsize, maxsubprobsize=1024) -> None:
-        """Re-sort the points for another method (1 or 2), bin size (tuple in
-        the library's x, y, z order) and subproblem cap; results unchanged."""
+        """Re-sort the points for another method (1, 2, or 5: type-1
+        cell-run spread), bin size (tuple in the library's x, y, z order) and
+        subproblem cap; results unchanged."""
         from cufinufft_gb300._cufinufft import _set_layout, _set_layoutf
         fn = _set_layout if self.dtype == np.float64 else _set_layoutf
         b = tuple(binsize) + (1,) * (3 - len(binsize))
@@ -241,7 +242,7 @@ class cufinufft:
         return f
 
     def set_layout_class(self, cls: int) -> None:
-        """Re-sort the points into one of the nine layout classes (the
+        """Re-sort the points into one of the twelve layout classes (the
         selector's and autotuner's candidates)."""
         from cufinufft_gb300._cufinufft import _set_layout_class, _set_layout_classf
         fn = _set_layout_class if self.dtype == np.float64 else _set_layout_classf

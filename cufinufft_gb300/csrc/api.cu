@@ -20,6 +20,9 @@
 #include "plan.h"
 #include "selector_weights.h"
 
+static_assert(sizeof(cfg::kSelParams) == sizeof(float) * CUFINUFFT_MLP_PARAMS,
+              "selector weights do not match the network shape");
+
 namespace cfg {
 
 // Defaults, restating CUFINUFFT_DEFAULT_OPTS (src/cufinufft.cu:639-730).
@@ -115,6 +118,16 @@ template <typename T> static void release(Plan<T>* p) {
   cudaFree(p->cls_count);
   p->cls_count = nullptr;
   p->cap_cls = 0;
+  cudaFree(p->cls_start);
+  cudaFree(p->cls_tmp);
+  p->cls_start = p->cls_tmp = nullptr;
+  p->cap_cls_start = 0;
+  cudaFree(p->sparse_count);
+  p->sparse_count = nullptr;
+  p->cap_sparse = 0;
+  cudaFree(p->sub_dense);
+  p->sub_dense = nullptr;
+  p->cap_sub_dense = 0;
   if (p->h_total) cudaFreeHost(p->h_total);
   p->h_total = nullptr;
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
@@ -392,6 +405,8 @@ static std::vector<LineArgs<T>> line_passes(const Plan<T>* p, cplx_t<T>* fk, int
   return v;
 }
 
+static int max_smem_optin(int device);
+
 template <typename T>
 static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int iflag, int ntransf,
                          double tol, int maxbatchsize, const cufinufft_opts* opts) {
@@ -425,7 +440,13 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   int bins_from_obin = 0;
   if (type == 1) {
     if (m == 1 || m == 2) p->method = m;
-    else if (m == 3 && dim == 2) p->method = 2;
+    else if (m == 3 && dim == 2) {
+      // the reference's method 3 sorts points by cell inside bins for
+      // clustered 2D data (src/2d/spread2d_wrapper_paul.cu); here it is the
+      // cell-run spread over cell-ordered points
+      p->method = 2;
+      p->cell_order = true;
+    }
     else if (m == 4 && dim == 3) { p->method = 2; bins_from_obin = 1; }
     else p->method = 0;
   } else {
@@ -456,6 +477,9 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   long long nbins = (long long)p->nb[0] * p->nb[1] * p->nb[2];
   if (nbins > (1LL << 24)) return CUFINUFFT_ERR_ARG;
   p->nbins = (int)nbins;
+  if (p->cell_order && (!cell_order_fits(p, p->bs, nbins) ||
+                        run_smem_bytes(p, p->bs) > (size_t)max_smem_optin(p->device)))
+    p->cell_order = false;  // too many (bin, cell) keys or taps: plain method 2
   if (p->method == 2 && p->opts.gpu_maxsubprobsize <= 0) return CUFINUFFT_ERR_ARG;
 
   p->iflag = iflag >= 0 ? 1 : -1;
@@ -530,10 +554,66 @@ static int select_layout(Plan<T>* p);
 // per (bin, class) counters, zeroed on the plan stream.  Plain bin order for
 // method 1, when the counters would exceed 2^24 ints, or with
 // CUFINUFFT_BANK_ORDER=0.
+// Cell order (cell = true): counters per (bin, cell) and their scan, for
+// the cell-run spread; the caller checks cell_order_fits first.
 template <typename T>
-static int bank_order(Plan<T>* p, int method, const int bs[3], int nbins, BankOrder* o) {
+static bool cell_order_fits(const Plan<T>* p, const int bs[3], long long nbins) {
+  long long cells = 1;
+  for (int k = 0; k < p->dim; ++k) cells *= bs[k];
+  long long taps = 1;
+  for (int k = 0; k < p->dim; ++k) taps *= p->sp.ns;
+  return p->type == 1 && taps <= 512 && nbins * cells <= (1LL << 24);
+}
+
+// Shared memory of the cell-run spread (run_bytes in spreadinterp.cuh).
+template <typename T>
+static size_t run_smem_bytes(const Plan<T>* p, const int bs[3]) {
+  return tile_cells(p->dim, p->sp.ns, bs) * 2 * sizeof(T) +
+         (size_t)(256 / 32) * 32 * (size_t)(p->dim * p->sp.ns) * sizeof(T) +
+         (size_t)(256 / 32) * 32 * sizeof(cplx_t<T>);
+}
+
+template <typename T>
+static int bank_order(Plan<T>* p, int method, const int bs[3], int nbins, BankOrder* o,
+                      bool cell = false) {
   std::memset(o, 0, sizeof(*o));
   if (method != 2) return 0;
+  if (cell) {
+    int cells = 1;
+    for (int k = 0; k < p->dim; ++k) cells *= bs[k];
+    const size_t n = (size_t)nbins * cells;
+    if (n > p->cap_cls) {
+      cudaFree(p->cls_count);
+      p->cls_count = nullptr;
+      p->cap_cls = 0;
+      CFG_CUDA(cudaMalloc(&p->cls_count, sizeof(int) * n));
+      p->cap_cls = n;
+    }
+    if (n > p->cap_cls_start) {
+      cudaFree(p->cls_start);
+      cudaFree(p->cls_tmp);
+      p->cls_start = p->cls_tmp = nullptr;
+      p->cap_cls_start = 0;
+      CFG_CUDA(cudaMalloc(&p->cls_start, sizeof(int) * (n + 1)));
+      CFG_CUDA(cudaMalloc(&p->cls_tmp, sizeof(int) * (size_t)scan_tmp_ints((int)n)));
+      p->cap_cls_start = n;
+    }
+    if ((size_t)nbins > p->cap_sparse) {
+      cudaFree(p->sparse_count);
+      p->sparse_count = nullptr;
+      p->cap_sparse = 0;
+      CFG_CUDA(cudaMalloc(&p->sparse_count, sizeof(int) * (size_t)nbins));
+      p->cap_sparse = nbins;
+    }
+    CFG_CUDA(cudaMemsetAsync(p->cls_count, 0, sizeof(int) * n, p->stream));
+    CFG_CUDA(cudaMemsetAsync(p->sparse_count, 0, sizeof(int) * (size_t)nbins, p->stream));
+    o->cls_count = p->cls_count;
+    o->ncls = cells;
+    o->cell_order = 1;
+    o->cls_start = p->cls_start;
+    o->sparse_count = p->sparse_count;
+    return 0;
+  }
   // only the one-thread-per-point tile kernels gain: interpolation by default,
   // spreading only when forced to that variant (the warp-cooperative spread,
   // measured on clustered 3D points, is slower with this order)
@@ -558,6 +638,9 @@ static int bank_order(Plan<T>* p, int method, const int bs[3], int nbins, BankOr
   o->ty = p->dim > 1 ? bs[1] + p->sp.ns - 1 : 1;
   return 0;
 }
+
+template <typename T>
+static int build_subproblems(Plan<T>* p);
 
 template <typename T>
 static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
@@ -591,27 +674,17 @@ static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
     CFG_CUDA(launch_place_unsorted<T>(a, p->stream));
   } else {
     CFG_CUDA(cudaMemsetAsync(p->count, 0, sizeof(int) * (size_t)p->nbins, p->stream));
-    e = bank_order(p, p->method, p->bs, p->nbins, &a.bank);
+    e = bank_order(p, p->method, p->bs, p->nbins, &a.bank, p->cell_order);
     if (e) return e;
     CFG_CUDA(launch_bin_count<T>(a, p->stream));
     CFG_CUDA(launch_scan(p->count, p->start, p->nbins, 0, 1, p->scan_tmp, p->stream));
+    if (a.bank.cell_order)
+      CFG_CUDA(launch_scan(p->cls_count, p->cls_start, p->nbins * a.bank.ncls, 2, kDenseRun, p->cls_tmp,
+                           p->stream));
     CFG_CUDA(launch_permute<T>(a, p->stream));
     if (p->method == 2) {
-      const int ms = p->opts.gpu_maxsubprobsize;
-      CFG_CUDA(launch_scan(p->count, p->sub_start, p->nbins, 1, ms, p->scan_tmp, p->stream));
-      CFG_CUDA(cudaMemcpyAsync(p->h_total, p->sub_start + p->nbins, sizeof(int),
-                               cudaMemcpyDeviceToHost, p->stream));
-      CFG_CUDA(cudaStreamSynchronize(p->stream));
-      const int nsub = *p->h_total;
-      if ((size_t)nsub > p->cap_sub) {
-        cudaFree(p->sub_to_bin);
-        p->sub_to_bin = nullptr;
-        p->cap_sub = 0;
-        CFG_CUDA(cudaMalloc(&p->sub_to_bin, sizeof(int) * (size_t)nsub));
-        p->cap_sub = nsub;
-      }
-      CFG_CUDA(launch_sub_to_bin(p->sub_start, p->nbins, nsub, p->sub_to_bin, p->stream));
-      p->nsub = nsub;
+      e = build_subproblems(p);
+      if (e) return e;
     }
   }
   CFG_CUDA(cudaGetLastError());
@@ -762,6 +835,7 @@ static void fill_info(const Plan<T>* p, cufinufft_plan_info* info) {
   info->beta = p->sp.beta;
   info->es_c = p->sp.c;
   info->line_fft = p->line_fft ? 1 : 0;
+  info->cell_order = p->cell_order ? 1 : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -803,6 +877,32 @@ static int build_subproblems(Plan<T>* p) {
   }
   CFG_CUDA(launch_sub_to_bin(p->sub_start, p->nbins, nsub, p->sub_to_bin, p->stream));
   p->nsub = nsub;
+  if (p->cell_order) {
+    if ((size_t)nsub > p->cap_sub_dense) {
+      cudaFree(p->sub_dense);
+      p->sub_dense = nullptr;
+      p->cap_sub_dense = 0;
+      CFG_CUDA(cudaMalloc(&p->sub_dense, (size_t)nsub));
+      p->cap_sub_dense = nsub;
+    }
+    SubClassArgs c;
+    std::memset(&c, 0, sizeof(c));
+    c.sub_to_bin = p->sub_to_bin;
+    c.sub_start = p->sub_start;
+    c.start = p->start;
+    c.cls_count = p->cls_count;
+    for (int k = 0; k < 3; ++k) {
+      c.i0[k] = p->i0[k];
+      c.bs[k] = p->bs[k];
+    }
+    c.dim = p->dim;
+    c.maxsub = ms;
+    c.ncls = 1;
+    for (int k = 0; k < p->dim; ++k) c.ncls *= p->bs[k];
+    c.nsub = nsub;
+    c.dense = p->sub_dense;
+    CFG_CUDA(launch_classify_subproblems(c, p->stream));
+  }
   return 0;
 }
 
@@ -812,6 +912,12 @@ static int build_subproblems(Plan<T>* p) {
 template <typename T>
 static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub) {
   if (!p->planned) return CUFINUFFT_ERR_GENERIC;
+  // method 5: method 2 spreading over cell-ordered points (cell-run kernel)
+  const bool cell = method == 5;
+  if (cell) {
+    if (p->type != 1) return CUFINUFFT_ERR_METHOD;
+    method = 2;
+  }
   if (method != 1 && method != 2) return CUFINUFFT_ERR_METHOD;
   if (method == 2 && p->type == 2 && p->dim == 1) return CUFINUFFT_ERR_METHOD;
   if (method == 2 && maxsub <= 0) return CUFINUFFT_ERR_ARG;
@@ -832,6 +938,8 @@ static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub)
   if (method == 2 && tile_cells(p->dim, p->sp.ns, bs) * sizeof(cplx_t<T>) >
                          (size_t)max_smem_optin(p->device))
     return CUFINUFFT_ERR_SHMEM;
+  if (cell && !cell_order_fits(p, bs, nbins)) return CUFINUFFT_ERR_ARG;
+  if (cell && run_smem_bytes(p, bs) > (size_t)max_smem_optin(p->device)) return CUFINUFFT_ERR_SHMEM;
   int e = alloc_bins(p, (int)nbins);
   if (e) return e;
   if (p->pts_set && p->M > 0) {
@@ -861,11 +969,14 @@ static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub)
     a.count = p->count;
     a.rank = p->rank;
     a.start = p->start;
-    e = bank_order(p, method, bs, (int)nbins, &a.bank);
+    e = bank_order(p, method, bs, (int)nbins, &a.bank, cell);
     if (e) return e;
     CFG_CUDA(cudaMemsetAsync(p->count, 0, sizeof(int) * (size_t)nbins, p->stream));
     CFG_CUDA(launch_rebin_count<T>(a, p->stream));
     CFG_CUDA(launch_scan(p->count, p->start, (int)nbins, 0, 1, p->scan_tmp, p->stream));
+    if (a.bank.cell_order)
+      CFG_CUDA(launch_scan(p->cls_count, p->cls_start, (int)nbins * a.bank.ncls, 2, kDenseRun, p->cls_tmp,
+                           p->stream));
     CFG_CUDA(launch_rebin_permute<T>(a, p->stream));
     CFG_CUDA(cudaStreamSynchronize(p->stream));
     cudaFree(p->idx);
@@ -878,8 +989,9 @@ static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub)
     }
   }
   p->method = method;
+  p->cell_order = cell;
   p->sort = 1;
-  p->opts.gpu_method = method;
+  p->opts.gpu_method = cell ? 5 : method;
   p->opts.gpu_sort = 1;
   for (int k = 0; k < 3; ++k) {
     p->bs[k] = bs[k];
@@ -934,12 +1046,13 @@ static int time_stage(Plan<T>* p, cplx_t<T>* scratch, int reps, float* ms) {
 
 // The layout classes the autotuner times and the learned selector chooses
 // among, in a fixed order: 0-2 method 1 with small / medium / large bins,
-// 3-8 method 2 with small / medium / large bins x subproblem cap 256 / 1024.
+// 3-8 method 2 with small / medium / large bins x subproblem cap 256 / 1024,
+// 9-11 method 5 (cell-run spread, type 1) with small / medium / large bins.
 // Bin shapes per dimension: 1D 256 / 1024 / 4096; 2D 16^2 / 32^2 / 64^2;
 // 3D 8x8x8 / 16x16x2 / 16x16x4 (clamped to the fine grid).  A class the plan
-// cannot run (method 2 for 1D type 2, a tile beyond shared memory) has
-// ms = -2.
-constexpr int kLayoutClasses = 9;
+// cannot run (method 2 for 1D type 2, method 5 for type 2 or past its
+// limits, a tile beyond shared memory) has ms = -2.
+constexpr int kLayoutClasses = 12;
 
 template <typename T>
 static cufinufft_tune_entry layout_class(const Plan<T>* p, int cls) {
@@ -947,19 +1060,25 @@ static cufinufft_tune_entry layout_class(const Plan<T>* p, int cls) {
                                       {{16, 16, 1}, {32, 32, 1}, {64, 64, 1}},
                                       {{8, 8, 8}, {16, 16, 2}, {16, 16, 4}}};
   cufinufft_tune_entry e;
-  e.method = cls < 3 ? 1 : 2;
-  const int shape = cls < 3 ? cls : (cls - 3) / 2;
+  e.method = cls < 3 ? 1 : (cls < 9 ? 2 : 5);
+  const int shape = cls < 3 ? cls : (cls < 9 ? (cls - 3) / 2 : cls - 9);
   const int* sh = shapes[p->dim - 1][shape];
   e.binsizex = std::min(sh[0], p->nf[0]);
   e.binsizey = p->dim > 1 ? std::min(sh[1], p->nf[1]) : 1;
   e.binsizez = p->dim > 2 ? std::min(sh[2], p->nf[2]) : 1;
-  e.maxsubprobsize = cls < 3 ? 1024 : ((cls - 3) % 2 == 0 ? 256 : 1024);
+  e.maxsubprobsize = (cls < 3 || cls >= 9) ? 1024 : ((cls - 3) % 2 == 0 ? 256 : 1024);
   e.ms = -1.f;
   int bs[3] = {e.binsizex, e.binsizey, e.binsizez};
-  if (e.method == 2 && p->type == 2 && p->dim == 1) e.ms = -2.f;
-  if (e.method == 2 && tile_cells(p->dim, p->sp.ns, bs) * sizeof(cplx_t<T>) >
+  if (e.method != 1 && p->type == 2 && p->dim == 1) e.ms = -2.f;
+  if (e.method != 1 && tile_cells(p->dim, p->sp.ns, bs) * sizeof(cplx_t<T>) >
                            (size_t)max_smem_optin(p->device))
     e.ms = -2.f;
+  if (e.method == 5) {
+    long long nbins = 1;
+    for (int k = 0; k < p->dim; ++k) nbins *= (p->nf[k] + bs[k] - 1) / bs[k];
+    if (!cell_order_fits(p, bs, nbins) || run_smem_bytes(p, bs) > (size_t)max_smem_optin(p->device))
+      e.ms = -2.f;
+  }
   return e;
 }
 
@@ -1078,7 +1197,7 @@ static int features_impl(Plan<T>* p, float* f) {
 template <typename T>
 static int apply_layout_class(Plan<T>* p, int cls);
 
-// gpu_method 0 with a trained network: predict the nine classes' relative
+// gpu_method 0 with a trained network: predict the twelve classes' relative
 // times from the plan's features and switch to the fastest runnable one.
 template <typename T>
 static int select_layout(Plan<T>* p) {

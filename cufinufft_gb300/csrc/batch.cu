@@ -158,6 +158,15 @@ static int batch_make(Batch<T>* b, int nplans, Plan<T>** plans) {
       D.bins.maxsub = p->opts.gpu_maxsubprobsize;
       blk += (long long)p->nsub * p->ntransf;
       b->smem = std::max(b->smem, tile_cells(p->dim, p->sp.ns, p->bs) * sizeof(cplx_t<T>));
+      if (b->type == 1 && p->cell_order && p->sub_dense) {
+        D.sub_dense = p->sub_dense;
+        BinTables bt;
+        std::memset(&bt, 0, sizeof(bt));
+        for (int k = 0; k < 3; ++k) bt.bs[k] = p->bs[k];
+        const size_t rb = p->dim == 1 ? run_bytes<T, 1>(p->sp.ns, bt)
+                          : (p->dim == 2 ? run_bytes<T, 2>(p->sp.ns, bt) : run_bytes<T, 3>(p->sp.ns, bt));
+        b->smem_run = std::max(b->smem_run, rb);
+      }
     }
     row += (b->type == 1 ? (long long)p->N[1] * p->N[2] : (long long)p->nf[1] * p->nf[2]) * p->ntransf;
   }

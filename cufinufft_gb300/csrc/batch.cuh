@@ -45,6 +45,7 @@ template <typename T> struct BatchDesc {
   long long blk0;           // first subproblem-block task of this plan (method 2 plans)
   BinTables bins;           // bin tables (method 2 plans)
   int method;
+  const unsigned char* sub_dense;  // cell-run layout: subproblems for k_batch_spread_run
 };
 
 // Largest plan index p whose first task of the given kind is <= task
@@ -278,6 +279,7 @@ k_batch_spread_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
     const long long local = task - P.blk0;
     const int t = (int)(local / P.bins.nsub);
     const int sub = (int)(local - (long long)t * P.bins.nsub);
+    if (P.sub_dense && P.sub_dense[sub]) continue;  // cell-run layout: k_batch_spread_run
     const SubTile st = sub_tile<DIM, NS>(P.bins, sub);
     T* re = reinterpret_cast<T*>(smem_raw);  // real plane, then imaginary plane
     T* im = re + st.ntile;
@@ -317,6 +319,49 @@ k_batch_spread_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
         }
       }
     }
+    __syncthreads();
+    GridGeom gg;
+    gg.nf[0] = P.nf[0];
+    gg.nf[1] = P.nf[1];
+    gg.nf[2] = P.nf[2];
+    gg.Nf = P.Nf;
+    plane_flush<T>(re, im, P.fw + (size_t)t * P.Nf, st, gg);
+  }
+}
+
+// Cell-run spreading (as k_spread_sm_run) over the dense subproblems of the
+// plans in the cell-run layout; their other subproblems go through
+// k_batch_spread_sm.
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_batch_spread_run(const BatchDesc<T>* D, int nplans, long long nblocks) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  for (long long task = blockIdx.x; task < nblocks; task += gridDim.x) {
+    const BatchDesc<T>& P = D[find_plan(D, nplans, task, 2)];
+    const long long local = task - P.blk0;
+    const int t = (int)(local / P.bins.nsub);
+    const int sub = (int)(local - (long long)t * P.bins.nsub);
+    if (!(P.sub_dense && P.sub_dense[sub])) continue;
+    const SubTile st = sub_tile<DIM, NS>(P.bins, sub);
+    T* re = reinterpret_cast<T*>(smem_raw);
+    T* im = re + st.ntile;
+    __syncthreads();  // the previous task's flush is done with the tile
+    for (int i = threadIdx.x; i < 2 * st.ntile; i += blockDim.x) re[i] = T(0);
+    __syncthreads();
+    SortedPts<T> pts;
+    pts.idx = P.idx;
+    for (int k = 0; k < 3; ++k) {
+      pts.i0[k] = P.i0[k];
+      pts.d[k] = P.d[k];
+    }
+    pts.M = P.M;
+    run_subproblem<T, DIM, NS>(
+        st, re, im, pts, P.c_in + (size_t)t * P.M,
+        [&](T dv, T* out) {
+#pragma unroll
+          for (int j = 0; j < NS; ++j) out[j] = batch_tap<T, NS>(dv, j, P);
+        },
+        [&](T dv, int j) { return batch_tap<T, NS>(dv, j, P); });
     __syncthreads();
     GridGeom gg;
     gg.nf[0] = P.nf[0];
@@ -403,6 +448,7 @@ template <typename T> struct Batch {
   BatchDesc<T>* d_desc = nullptr;
   long long ntasks = 0, nrows = 0, nblocks = 0;
   size_t smem = 0;  // largest method-2 tile
+  size_t smem_run = 0;  // largest cell-run footprint (0: no plan in that layout)
   cudaStream_t stream = nullptr;
   // side streams: the method-2 spread/interp and the per-plan FFTs run on
   // parallel branches of the captured graph
@@ -466,6 +512,14 @@ inline cudaError_t batch_spreadinterp_dim(Batch<T>* b, int n, long long ntasks) 
         if (fe != cudaSuccess) return fe;                                                         \
         k_batch_spread_sm<T, DIM, NSV><<<gb, kSpreadThreads, b->smem, b->side[0]>>>(b->d_desc, n, \
                                                                                   b->nblocks);   \
+        if constexpr (run_ok<DIM, NSV>()) {                                                       \
+          if (b->smem_run > 0) {                                                                  \
+            fe = prepare_smem(k_batch_spread_run<T, DIM, NSV>, b->smem_run);                      \
+            if (fe != cudaSuccess) return fe;                                                     \
+            k_batch_spread_run<T, DIM, NSV><<<gb, kSpreadThreads, b->smem_run, b->side[1]>>>(     \
+                b->d_desc, n, b->nblocks);                                                        \
+          }                                                                                       \
+        }                                                                                         \
       }                                                                                           \
     } else {                                                                                      \
       if (ntasks > 0)                                                                             \

@@ -22,10 +22,21 @@ cudaError_t interp_dim(int method, int ns, const SpreadArgs<T>& a, cudaStream_t 
 // bin differ in class and a half-warp's tile accesses (first tap + the same
 // offset for every point) fall in distinct banks.  cls_count == nullptr
 // keeps plain bin order.
+//
+// cell_order = 1 instead groups a bin's points for the cell-run spread (class
+// = cell index inside the bin, ncls = cells per bin): points on cells holding
+// at least 32 points first, sorted by cell, then the others in arbitrary
+// order; cls_start is the exclusive scan of those dense counts over all
+// (bin, cell) keys, sparse_count a per-bin counter for the others.
+constexpr int kDenseRun = 32;  // points on one cell that make it dense (one warp chunk)
+
 struct BankOrder {
   int* cls_count;   // [nbins * ncls], zeroed before counting
-  int ncls;         // power of two
+  int ncls;         // power of two (bank classes) or cells per bin
   int tx, ty;       // tile row length and rows per plane (bin size + ns - 1)
+  int cell_order;
+  const int* cls_start;  // [nbins * ncls + 1] (cell_order only)
+  int* sparse_count;     // [nbins], zeroed before permuting (cell_order only)
 };
 
 template <typename T> struct PlaceArgs {
@@ -74,11 +85,25 @@ cudaError_t launch_feature_count(int dim, int M, const int* const i0[3], const i
                                  const int nb[3], int* counts, cudaStream_t s);
 
 // Exclusive scan of n ints: out[0..n] (out[n] = total).  mode 0 scans the
-// values, mode 1 scans ceil(v / div).  tmp needs scan_tmp_ints(n) ints.
+// values, mode 1 scans ceil(v / div), mode 2 scans v where v >= div (else
+// 0).  tmp needs scan_tmp_ints(n) ints.
 int scan_tmp_ints(int n);
 cudaError_t launch_scan(const int* in, int* out, int n, int mode, int div, int* tmp,
                         cudaStream_t s);
 // sub_to_bin[s] = the bin b with sub_start[b] <= s < sub_start[b+1].
+// Cell order: flag the subproblems whose first point lies on a dense cell
+// (those go to the cell-run kernel, the others to the warp-cooperative one).
+struct SubClassArgs {
+  const int* sub_to_bin;
+  const int* sub_start;
+  const int* start;
+  const int* i0[3];
+  const int* cls_count;
+  int bs[3];
+  int dim, maxsub, ncls, nsub;
+  unsigned char* dense;
+};
+cudaError_t launch_classify_subproblems(const SubClassArgs& a, cudaStream_t s);
 cudaError_t launch_sub_to_bin(const int* sub_start, int nbins, int nsub, int* sub_to_bin,
                               cudaStream_t s);
 

@@ -1,7 +1,7 @@
 // mlp.cu -- the learned layout selector's network: a 3-layer perceptron with
 // hand-written CUDA forward, backward and Adam kernels (FP32).
 //
-// Architecture (fixed): features F=14 -> H=32 (ReLU) -> H=32 (ReLU) -> K=9.
+// Architecture (fixed): features F=14 -> H=32 (ReLU) -> H=32 (ReLU) -> K=12.
 // Output k predicts log2(time of layout class k / time of the fastest class)
 // for the workload the features describe; the selector picks the argmin over
 // the classes the plan can run.  Parameters are one flat FP32 array:

@@ -85,6 +85,8 @@ template <typename T> struct SpreadArgs {
   int ntr;
   int M;
   int variant;              // kernel family: 0 default, 1 one thread per point, 2 warp-cooperative
+  int run;                  // method 2 spreading over cell-ordered points (cell-run kernel)
+  const unsigned char* sub_dense;  // run: subproblems that start on a dense cell
 };
 
 // Cells of one subproblem tile: the bin plus the ns-1 cells its points

@@ -24,6 +24,7 @@ template <typename T> struct Plan {
   cufinufft_opts opts;
   SpreaderParams sp{};
   int method = 0;  // method run: 1 (NU-point driven) or 2 (subproblem); 0 = invalid
+                   // (layout method 5 = method 2 with cell_order, see set_layout)
   int variant = 0; // kernel family: 0 default, 1 one thread per point, 2 warp-cooperative
   bool auto_method = false;  // gpu_method 0: chosen by the library
   float* sel_buf = nullptr;  // selector network parameters and scratch (device)
@@ -58,8 +59,16 @@ template <typename T> struct Plan {
   int* scan_tmp = nullptr;
   int* sub_to_bin = nullptr;
   size_t cap_sub = 0;
-  int* cls_count = nullptr;  // per (bin, bank class) counts for method 2 ordering
+  int* cls_count = nullptr;  // per (bin, class) counts for method 2 ordering
   size_t cap_cls = 0;
+  bool cell_order = false;   // method 2 spreading over cell-ordered points (cell-run kernel)
+  int* cls_start = nullptr;  // scanned (bin, cell) counts (cell order)
+  int* cls_tmp = nullptr;    // scan scratch for cls_start
+  size_t cap_cls_start = 0;
+  int* sparse_count = nullptr;  // per-bin counter of the points on sparse cells
+  size_t cap_sparse = 0;
+  unsigned char* sub_dense = nullptr;  // per subproblem: starts on a dense cell (cell order)
+  size_t cap_sub_dense = 0;
   int* h_total = nullptr;  // pinned readback of the subproblem count
   // stage timing (extension): events recorded around each stage of execute
   bool timing = false;
@@ -163,6 +172,8 @@ inline SpreadArgs<T> spread_args(Plan<T>* p) {
   a.g.Nf = grid_cells(p);
   a.M = p->M;
   a.variant = p->variant;
+  a.run = (p->cell_order && p->type == 1 && p->method == 2) ? 1 : 0;
+  a.sub_dense = a.run ? p->sub_dense : nullptr;
   return a;
 }
 

@@ -42,6 +42,22 @@ __device__ __forceinline__ int bank_class(const BankOrder& o, const int* bs, int
   return (lx + o.tx * (ly + o.ty * lz)) & (o.ncls - 1);
 }
 
+// Class of a point inside its bin: its bank class, or its cell (cell order).
+__device__ __forceinline__ int order_class(const BankOrder& o, const int* bs, int dim, const int i0[3]) {
+  if (!o.cell_order) return bank_class(o, bs, dim, i0);
+  const int lx = i0[0] % bs[0];
+  const int ly = dim > 1 ? i0[1] % bs[1] : 0;
+  const int lz = dim > 2 ? i0[2] % bs[2] : 0;
+  return lx + bs[0] * (ly + bs[1] * lz);
+}
+
+// Position of a ranked point: cell order reads the scanned (bin, cell)
+// starts; bank order interleaves inside the bin.
+__device__ __forceinline__ int interleave_pos(const BankOrder& o, int b, int c, int r);
+__device__ __forceinline__ int ordered_pos(const BankOrder& o, const int* start, int b, int c, int r) {
+  return start[b] + interleave_pos(o, b, c, r);
+}
+
 // Warp-aggregated rank: one atomic per distinct key in the warp.
 __device__ __forceinline__ int agg_rank(unsigned act, int key, int* counter) {
   const int lane = threadIdx.x & 31;
@@ -51,6 +67,22 @@ __device__ __forceinline__ int agg_rank(unsigned act, int key, int* counter) {
   if (lane == leader) first = atomicAdd(counter, __popc(peers));
   first = __shfl_sync(peers, first, leader);
   return first + __popc(peers & ((1u << lane) - 1u));
+}
+
+// Cell order (BankOrder::cell_order): a bin's points on dense cells (at least
+// kDenseRun points) come first, sorted by cell -- cls_start is the exclusive
+// scan of the dense cells' counts only -- then the bin's other points in
+// arbitrary order, ranked by the per-bin counter sparse_count.  r is the
+// point's rank inside its cell.  Called by the lanes in act together.
+__device__ __forceinline__ int cell_position(const BankOrder& o, const int* start, unsigned act, int b,
+                                             int c, int r) {
+  const long long k0 = (long long)b * o.ncls;
+  const int bin0 = o.cls_start[k0];
+  const bool dense = o.cls_count[k0 + c] >= kDenseRun;
+  const unsigned sparse_lanes = __ballot_sync(act, !dense);
+  if (dense) return start[b] + (o.cls_start[k0 + c] - bin0) + r;
+  const int sr = agg_rank(sparse_lanes, b, o.sparse_count + b);
+  return start[b] + (o.cls_start[k0 + o.ncls] - bin0) + sr;
 }
 
 // Position inside its bin of the point ranked r in class c: round-robin over
@@ -80,7 +112,7 @@ __global__ void __launch_bounds__(kPlaceThreads) k_bin_count(PlaceArgs<T> a) {
     const int b = point_bin(a, i, i0, d);
     const int r = agg_rank(act, b, &a.count[b]);
     if (a.bank.cls_count) {
-      const int key = b * a.bank.ncls + bank_class(a.bank, a.bs, a.dim, i0);
+      const int key = b * a.bank.ncls + order_class(a.bank, a.bs, a.dim, i0);
       a.rank[i] = agg_rank(act, key, a.bank.cls_count + key);
     } else {
       a.rank[i] = r;
@@ -90,13 +122,21 @@ __global__ void __launch_bounds__(kPlaceThreads) k_bin_count(PlaceArgs<T> a) {
 
 template <typename T>
 __global__ void __launch_bounds__(kPlaceThreads) k_permute(PlaceArgs<T> a) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += gridDim.x * blockDim.x) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  // warp-uniform trip count: cell order ranks sparse points warp-aggregated
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < a.M; base += stride) {
+    const long long ii = base + threadIdx.x;
+    const bool active = ii < a.M;
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!active) continue;
+    const int i = (int)ii;
     int i0[3];
     T d[3];
     const int b = point_bin(a, i, i0, d);
-    const int pos = a.start[b] + (a.bank.cls_count
-                                      ? interleave_pos(a.bank, b, bank_class(a.bank, a.bs, a.dim, i0), a.rank[i])
-                                      : a.rank[i]);
+    int pos;
+    if (!a.bank.cls_count) pos = a.start[b] + a.rank[i];
+    else if (a.bank.cell_order) pos = cell_position(a.bank, a.start, act, b, order_class(a.bank, a.bs, a.dim, i0), a.rank[i]);
+    else pos = ordered_pos(a.bank, a.start, b, order_class(a.bank, a.bs, a.dim, i0), a.rank[i]);
     a.idx[pos] = i;
     for (int k = 0; k < 3; ++k) {
       if (k < a.dim) {
@@ -181,7 +221,7 @@ __global__ void __launch_bounds__(kPlaceThreads) k_rebin_count(RebinArgs<T> a) {
     const int r = agg_rank(act, b, &a.count[b]);
     if (a.bank.cls_count) {
       const int i0[3] = {a.src_i0[0][i], a.dim > 1 ? a.src_i0[1][i] : 0, a.dim > 2 ? a.src_i0[2][i] : 0};
-      const int key = b * a.bank.ncls + bank_class(a.bank, a.bs, a.dim, i0);
+      const int key = b * a.bank.ncls + order_class(a.bank, a.bs, a.dim, i0);
       a.rank[i] = agg_rank(act, key, a.bank.cls_count + key);
     } else {
       a.rank[i] = r;
@@ -191,14 +231,21 @@ __global__ void __launch_bounds__(kPlaceThreads) k_rebin_count(RebinArgs<T> a) {
 
 template <typename T>
 __global__ void __launch_bounds__(kPlaceThreads) k_rebin_permute(RebinArgs<T> a) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += gridDim.x * blockDim.x) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = (long long)blockIdx.x * blockDim.x; base < a.M; base += stride) {
+    const long long ii = base + threadIdx.x;
+    const bool active = ii < a.M;
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!active) continue;
+    const int i = (int)ii;
     const int b = stored_bin(a, i);
-    int pos = a.rank[i];
+    int pos = a.start[b] + a.rank[i];
     if (a.bank.cls_count) {
       const int i0[3] = {a.src_i0[0][i], a.dim > 1 ? a.src_i0[1][i] : 0, a.dim > 2 ? a.src_i0[2][i] : 0};
-      pos = interleave_pos(a.bank, b, bank_class(a.bank, a.bs, a.dim, i0), pos);
+      const int c = order_class(a.bank, a.bs, a.dim, i0);
+      pos = a.bank.cell_order ? cell_position(a.bank, a.start, act, b, c, a.rank[i])
+                              : ordered_pos(a.bank, a.start, b, c, a.rank[i]);
     }
-    pos += a.start[b];
     a.idx[pos] = a.src_idx[i];
     for (int k = 0; k < 3; ++k) {
       if (k < a.dim) {
@@ -273,6 +320,7 @@ constexpr int kScanMaxBlocks = 4096;
 __device__ __forceinline__ int scan_load(const int* in, int i, int n, int mode, int div) {
   if (i >= n) return 0;
   int v = in[i];
+  if (mode == 2) return v >= div ? v : 0;  // counts of at least div only
   return mode == 1 ? (v + div - 1) / div : v;
 }
 
@@ -372,6 +420,26 @@ cudaError_t launch_scan(const int* in, int* out, int n, int mode, int div, int* 
   k_scan_partial<<<nb, kScanThreads, 0, s>>>(in, n, mode, div, tmp);
   k_scan_partials<<<1, kScanThreads, 0, s>>>(tmp, nb);
   k_scan_final<<<nb, kScanThreads, 0, s>>>(in, n, mode, div, tmp, out);
+  return cudaGetLastError();
+}
+
+__global__ void k_classify_subproblems(SubClassArgs a) {
+  for (int sidx = blockIdx.x * blockDim.x + threadIdx.x; sidx < a.nsub; sidx += gridDim.x * blockDim.x) {
+    const int b = a.sub_to_bin[sidx];
+    const int p0 = a.start[b] + (sidx - a.sub_start[b]) * a.maxsub;
+    const int lx = a.i0[0][p0] % a.bs[0];
+    const int ly = a.dim > 1 ? a.i0[1][p0] % a.bs[1] : 0;
+    const int lz = a.dim > 2 ? a.i0[2][p0] % a.bs[2] : 0;
+    const int c = lx + a.bs[0] * (ly + a.bs[1] * lz);
+    a.dense[sidx] = a.cls_count[(long long)b * a.ncls + c] >= kDenseRun ? 1 : 0;
+  }
+}
+
+cudaError_t launch_classify_subproblems(const SubClassArgs& a, cudaStream_t s) {
+  if (a.nsub <= 0) return cudaSuccess;
+  int blocks = (a.nsub + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  k_classify_subproblems<<<blocks, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

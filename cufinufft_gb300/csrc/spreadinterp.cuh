@@ -460,6 +460,7 @@ k_spread_sm_wc(SpreadArgs<T> a) {
   constexpr int PPW = 32 / L;
   constexpr int NY = DIM > 1 ? NS : 1;
   constexpr int NZ = DIM > 2 ? NS : 1;
+  if (a.sub_dense && a.sub_dense[blockIdx.x]) return;  // cell-run layout: done by k_spread_sm_run
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
   T* re = reinterpret_cast<T*>(smem_raw);
@@ -502,6 +503,197 @@ k_spread_sm_wc(SpreadArgs<T> a) {
   }
   __syncthreads();
   plane_flush<T>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g);
+}
+
+// ---------------------------------------------------------------------------
+// Cell-run spreading (method 2 over cell-ordered points, a layout class of
+// its own).  setpts sorts a bin's points by first-tap cell, so dense regions
+// arrive as long runs of points that all add into the same ns^d cells.  A
+// warp walks its slice of the subproblem in chunks of 32 points.  A chunk
+// whose points share one cell is summed in registers -- lane l takes the
+// taps l, l + 32, ..., four at a time -- from the points' kernel values
+// staged in warp-private shared memory, then each tap sum is added to the
+// tile once (conflict-free: the lanes' taps differ).  Any other chunk is
+// spread point by point with shared atomics, lanes over x taps as in
+// k_spread_sm_wc.  Dense chunks thus cost FMAs instead of 2 ns^d
+// same-address atomics per point.  Taps per point <= 512.  Subproblems that
+// start on a sparse cell are left to k_spread_sm_wc (its higher occupancy
+// wins there), launched beside this kernel.
+template <int DIM, int NS> constexpr int run_taps() {
+  return DIM == 1 ? NS : (DIM == 2 ? NS * NS : NS * NS * NS);
+}
+template <int DIM, int NS> constexpr bool run_ok() { return run_taps<DIM, NS>() <= 512; }
+
+// One subproblem of the cell-run spread into the zeroed tile planes re/im
+// (shared by the per-plan and the multi-plan kernels): krow(d, out) writes a
+// point's NS kernel values along one axis, ktap(d, j) returns one of them.
+template <typename T, int DIM, int NS, class KRow, class KTap>
+__device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, const SortedPts<T>& pts,
+                                               const cplx_t<T>* cin, KRow krow, KTap ktap) {
+  using C = cplx_t<T>;
+  constexpr int NT = run_taps<DIM, NS>();
+  constexpr int KV = DIM * NS;
+  constexpr int NWARP = kSpreadThreads / 32;
+  constexpr int GK = 4;                            // taps per lane per pass over a chunk
+  constexpr int NPASS = (NT + 32 * GK - 1) / (32 * GK);
+  constexpr int L = spread_lanes<NS>();
+  constexpr int PPW = 32 / L;
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* kvw = im + st.ntile + warp * 32 * KV;  // staged kernel values of a dense chunk
+  C* cvw = reinterpret_cast<C*>(im + st.ntile + NWARP * 32 * KV) + warp * 32;
+  const int t = blockIdx.y;
+  for (int i = threadIdx.x; i < 2 * st.ntile; i += blockDim.x) re[i] = T(0);
+  __syncthreads();
+  const int S = (((st.np + NWARP - 1) / NWARP) + 31) & ~31;
+  const int beg = warp * S;
+  const int end = min(st.np, beg + S);
+  // The cursor follows the runs: a window of 32 points whose leading run
+  // (points on the window's first cell) has at least kMinRun points is
+  // accumulated -- the run's first n <= 32 points -- and the cursor moves by
+  // n, so the next window starts at a run boundary; any other window is
+  // spread point by point and the cursor moves by 32.
+  constexpr int kMinRun = 16;
+  int cs = beg;
+  while (cs < end) {  // warp-uniform
+    const int ql = cs + lane;
+    const bool valid = ql < end;
+    const int p = st.p0 + (valid ? ql : cs);
+    const int lx = pts.i0[0][p] - st.ox;
+    const int ly = DIM > 1 ? pts.i0[1][p] - st.oy : 0;
+    const int lz = DIM > 2 ? pts.i0[2][p] - st.oz : 0;
+    const int key = lx + st.TX * (ly + st.TY * lz);
+    const int key0 = __shfl_sync(0xffffffffu, key, 0);
+    const unsigned same = __ballot_sync(0xffffffffu, valid && key == key0);
+    const int nrun = same == 0xffffffffu ? 32 : __ffs(~same) - 1;  // leading run length
+    if (nrun >= kMinRun) {
+      // run chunk: stage the first nrun points' kernel values, then every
+      // lane sums its taps over them, GK taps per pass, one add per tap
+      T kr[NS];
+      T* kv = kvw + lane * KV;
+      krow(pts.d[0][p], kr);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) kv[j] = kr[j];
+      if (DIM > 1) {
+        krow(pts.d[1][p], kr);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) kv[NS + j] = kr[j];
+      }
+      if (DIM > 2) {
+        krow(pts.d[2][p], kr);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) kv[2 * NS + j] = kr[j];
+      }
+      cvw[lane] = cin[pts.idx[p]];
+      __syncwarp();
+#pragma unroll 1
+      for (int pass = 0; pass < NPASS; ++pass) {
+        int ix[GK], iy[GK], iz[GK];
+        bool on[GK];
+        T ar[GK], ai[GK];
+#pragma unroll
+        for (int k = 0; k < GK; ++k) {
+          const int tt = lane + 32 * (pass * GK + k);
+          on[k] = tt < NT;
+          ix[k] = tt % NS;
+          iy[k] = NS + (tt / NS) % NS;
+          iz[k] = 2 * NS + tt / (NS * NS);
+          ar[k] = T(0);
+          ai[k] = T(0);
+        }
+#pragma unroll 4
+        for (int q = 0; q < nrun; ++q) {
+          const T* kq = kvw + q * KV;
+          const C cq = cvw[q];
+#pragma unroll
+          for (int k = 0; k < GK; ++k) {
+            T wgt = kq[on[k] ? ix[k] : 0];
+            if (DIM > 1) wgt *= kq[on[k] ? iy[k] : 0];
+            if (DIM > 2) wgt *= kq[on[k] ? iz[k] : 0];
+            ar[k] = fma_rn(cq.x, wgt, ar[k]);
+            ai[k] = fma_rn(cq.y, wgt, ai[k]);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < GK; ++k) {
+          if (on[k]) {
+            const int off = key0 + (ix[k] + st.TX * ((iy[k] - NS) + st.TY * (iz[k] - 2 * NS)));
+            atomicAdd(re + off, ar[k]);
+            atomicAdd(im + off, ai[k]);
+          }
+        }
+      }
+      __syncwarp();  // the staging area is rewritten by the next chunk
+      cs += nrun;
+    } else {
+      const int g = lane / L, j = lane % L;
+      const bool tap = j < NS;
+      const int jj = tap ? j : 0;
+      // cell-ordered neighbours overlap: group g takes points it + g * NIT,
+      // so the PPW points of one warp instruction lie far apart in the chunk
+      constexpr int NIT = (32 + PPW - 1) / PPW;
+      for (int it = 0; it < NIT; ++it) {  // warp-uniform
+        const int qq = it + g * NIT;
+        const bool v2 = g < PPW && qq < 32 && cs + qq < end;
+        const int p2 = st.p0 + (v2 ? cs + qq : cs);
+        const int lx2 = pts.i0[0][p2] - st.ox;
+        const T kx = ktap(pts.d[0][p2], jj);
+        T ky = T(1), kz = T(1);
+        int ly2 = 0, lz2 = 0;
+        if (DIM > 1) { ly2 = pts.i0[1][p2] - st.oy; ky = ktap(pts.d[1][p2], jj); }
+        if (DIM > 2) { lz2 = pts.i0[2][p2] - st.oz; kz = ktap(pts.d[2][p2], jj); }
+        const C v = cin[pts.idx[p2]];
+        const T vr = v.x * kx, vi = v.y * kx;
+        const int off0 = (lz2 * st.TY + ly2) * st.TX + lx2 + jj;
+#pragma unroll 1
+        for (int dz = 0; dz < NZ; ++dz) {
+          const T kzv = DIM > 2 ? __shfl_sync(0xffffffffu, kz, g * L + dz) : T(1);
+#pragma unroll
+          for (int dy = 0; dy < NY; ++dy) {
+            const T kyv = DIM > 1 ? __shfl_sync(0xffffffffu, ky, g * L + dy) : T(1);
+            const T w = kyv * kzv;
+            if (tap && v2) {
+              const int off = off0 + (dz * st.TY + dy) * st.TX;
+              atomicAdd(re + off, vr * w);
+              atomicAdd(im + off, vi * w);
+            }
+          }
+        }
+      }
+      cs += 32;
+    }
+  }
+}
+
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_spread_sm_run(SpreadArgs<T> a) {
+  constexpr int HD = horner_degree<T>(NS);
+  if (a.sub_dense && !a.sub_dense[blockIdx.x]) return;  // sparse: done by k_spread_sm_wc
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  T* re = reinterpret_cast<T*>(smem_raw);
+  T* im = re + st.ntile;
+  const int t = blockIdx.y;
+  for (int i = threadIdx.x; i < 2 * st.ntile; i += blockDim.x) re[i] = T(0);
+  __syncthreads();
+  const KernelCoeffs<T>& kc = a.kc;
+  run_subproblem<T, DIM, NS>(
+      st, re, im, a.pts, a.c_in + (size_t)t * a.M,
+      [&](T dv, T* out) { kernel_row<T, NS, HD>(dv, kc, out); },
+      [&](T dv, int j) { return kernel_tap<T, NS, HD>(dv, j, kc); });
+  __syncthreads();
+  plane_flush<T>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g);
+}
+
+// Shared memory of the cell-run kernel: the tile planes, the staged kernel
+// values and the strengths of every warp's dense chunk.
+template <typename T, int DIM>
+size_t run_bytes(int ns, const BinTables& bt) {
+  const size_t nw = kSpreadThreads / 32;
+  return tile_cells(DIM, ns, bt.bs) * 2 * sizeof(T) + nw * 32 * (size_t)(DIM * ns) * sizeof(T) +
+         nw * 32 * sizeof(cplx_t<T>);
 }
 
 template <typename T, int DIM, int NS>
@@ -605,6 +797,22 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
     }
   } else {
     if (a.bins.nsub == 0) return cudaSuccess;
+    if constexpr (run_ok<DIM, NS>()) {
+      if (a.run) {
+        // subproblems starting on a dense cell take the cell-run kernel, the
+        // others the warp-cooperative one (each kernel skips the other kind)
+        const size_t smw = tile_bytes<T, DIM>(NS, a.bins);
+        cudaError_t e = prepare_smem(k_spread_sm_wc<T, DIM, NS>, smw);
+        if (e != cudaSuccess) return e;
+        k_spread_sm_wc<T, DIM, NS><<<dim3(a.bins.nsub, a.ntr), kSpreadThreads, smw, s>>>(a);
+        const size_t sm = run_bytes<T, DIM>(NS, a.bins);
+        e = prepare_smem(k_spread_sm_run<T, DIM, NS>, sm);
+        if (e != cudaSuccess) return e;
+        k_spread_sm_run<T, DIM, NS><<<dim3(a.bins.nsub, a.ntr), kSpreadThreads, sm, s>>>(a);
+        return cudaGetLastError();
+      }
+    }
+    if (a.run) return cudaErrorInvalidValue;  // more than 512 taps per point
     size_t sm = tile_bytes<T, DIM>(NS, a.bins);
     cudaError_t e = wc ? prepare_smem(k_spread_sm_wc<T, DIM, NS>, sm)
                        : prepare_smem(k_spread_sm<T, DIM, NS>, sm);

@@ -1,9 +1,9 @@
 """Exhaustive timing sweep for the learned selector (runs on a GPU).
 
 For each seeded workload (workloads.spec) this makes a plan, sets its points,
-records the plan's features and times all nine layout classes with the
+records the plan's features and times all twelve layout classes with the
 library's autotuner (cufinufft[f]_autotune), then writes
-    features [n][14], times_ms [n][9] (-2: class not runnable), specs (json)
+    features [n][14], times_ms [n][12] (-2: class not runnable), specs (json)
 to an .npz file.
 
     python -m cufinufft_gb300.selector.sweep --n 2000 --out sweep.npz
@@ -40,7 +40,7 @@ def run(n: int, out: str, start: int = 0, device: int = 0, log_every: int = 50,
         except RuntimeError as exc:
             print(f"workload {i} skipped: {exc}", flush=True)
             continue
-        ms = [e["ms"] for e in entries[1:10]]
+        ms = [e["ms"] for e in entries[1:13]]
         feats.append(list(f))
         times.append(ms)
         specs.append(s)

@@ -1,7 +1,7 @@
 """Train the learned layout selector on a timing sweep (runs on a GPU).
 
 Inputs: the .npz written by selector/sweep.py (features [n][14], times_ms
-[n][9], -2 where a class cannot run).  Targets are log2(t_k / t_min) per
+[n][12], -2 where a class cannot run).  Targets are log2(t_k / t_min) per
 workload, masked where a class did not run.  Workloads 0..n_train-1 train,
 the rest are held out.  Features are standardised with the training set's
 mean and standard deviation.  Training is full-batch Adam on the library's

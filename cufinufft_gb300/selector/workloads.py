@@ -1,13 +1,13 @@
 """Seeded workloads for the learned layout selector (config 5).
 
 Each workload: dim in {1, 2, 3}; modes 2^6..2^12 per axis, capped so the fine
-grid holds at most 2^25 cells; M log-uniform in 1e4..1e7 (the sweep times nine
-layouts per workload, so M is capped below config 5's 1e8 to keep the sweep
-to minutes); FP32 or FP64; tol in {1e-3, 1e-6, 1e-9}; type 1 or 2; point
-distribution uniform, Gaussian clusters (1-8 centres, sigma log-uniform in
-0.005..1), radial (spokes through the centre; 1D: uniform), or a worst case
+grid holds at most 2^25 cells; M log-uniform in 1e4..1e8; FP32 or FP64; tol
+in {1e-3, 1e-6, 1e-9}; type 1 or 2; point distribution uniform, Gaussian
+clusters (1-8 centres, sigma log-uniform in 0.005..1), half uniform and half
+clustered, radial (spokes through the centre; 1D: uniform), or a worst case
 with every point inside one 8-cell box.  FP32 workloads draw tol = 1e-9 as
-1e-6, and M is capped so that M * ns^dim <= 2e9 kernel taps.  Points are generated on the device
+1e-6, and M is capped so that M * ns^dim <= 1.2e10 kernel taps (the sweep times
+twelve layouts per workload).  Points are generated on the device
 from a seeded generator.
 """
 from __future__ import annotations
@@ -16,9 +16,9 @@ import math
 
 import numpy as np
 
-KINDS = ("uniform", "clusters", "radial", "onebin")
+KINDS = ("uniform", "clusters", "radial", "onebin", "mixed")
 MAX_CELLS = 1 << 25
-MAX_TAPS = 2e9        # M * ns^dim cap, so the worst one-bin case times in milliseconds
+MAX_TAPS = 1.2e10     # M * ns^dim cap: the 3D 3.2e7-point workloads fit, the worst case stays ~0.1 s
 
 
 def spec(i: int, seed: int = 20261203) -> dict:
@@ -29,12 +29,12 @@ def spec(i: int, seed: int = 20261203) -> dict:
     if single and tol < 1e-6:
         tol = 1e-6        # below FP32's reach; the library would clamp it
     ntype = int(rng.integers(1, 3))
-    kind = KINDS[int(rng.integers(0, 4))]
+    kind = KINDS[int(rng.integers(0, len(KINDS)))]
     while True:
         modes = [int(2 ** rng.uniform(6, 12)) for _ in range(dim)]
         if np.prod([2 * m + 32 for m in modes]) <= MAX_CELLS:
             break
-    M = int(round(10 ** rng.uniform(4, 7)))
+    M = int(round(10 ** rng.uniform(4, 8)))
     ns = max(2, math.ceil(-math.log10(tol / 10)))
     M = min(M, int(MAX_TAPS // ns ** dim))
     return {"i": i, "dim": dim, "single": single, "tol": tol, "type": ntype, "kind": kind,
@@ -56,6 +56,16 @@ def points(s: dict, device):
 
     if s["kind"] == "uniform" or (s["kind"] == "radial" and dim == 1):
         pts = [unif(M) for _ in range(dim)]
+    elif s["kind"] == "mixed":  # half uniform, half in Gaussian clusters
+        k = s["nclusters"]
+        h = M // 2
+        centres = torch.rand(k, dim, generator=g, device=device, dtype=torch.float64) * two_pi - math.pi
+        which = torch.randint(0, k, (M - h,), generator=g, device=device)
+        pts = []
+        for d in range(dim):
+            x = centres[which, d] + s["sigma"] * torch.randn(M - h, generator=g, device=device,
+                                                              dtype=torch.float64)
+            pts.append(torch.cat([unif(h), torch.remainder(x + math.pi, two_pi) - math.pi]))
     elif s["kind"] == "clusters":
         k = s["nclusters"]
         centres = torch.rand(k, dim, generator=g, device=device, dtype=torch.float64) * two_pi - math.pi

@@ -104,7 +104,8 @@ typedef struct cufinufft_plan_info {
   int type, dim, ms, mt, mu, nf1, nf2, nf3, ns, M, ntransf, maxbatchsize;
   int method, sort, binsizex, binsizey, binsizez, nbins, nsubprob, kerevalmeth;
   double beta, es_c;
-  int line_fft; /* 1: pruned line FFTs (fftpass.cu), 0: cuFFT over the whole grid */
+  int line_fft;   /* 1: pruned line FFTs (fftpass.cu), 0: cuFFT over the whole grid */
+  int cell_order; /* 1: method 2 spreading over cell-ordered points (cell-run kernel) */
 } cufinufft_plan_info;
 int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info);
 int cufinufftf_get_info(cufinufftf_plan plan, cufinufft_plan_info* info);
@@ -121,14 +122,19 @@ int cufinufft_stage_times(cufinufft_plan plan, double* ms, long long* batches, i
 int cufinufftf_stage_times(cufinufftf_plan plan, double* ms, long long* batches, int reset);
 
 /* Layout and autotuning (no counterpart in the reference).  set_layout
- * switches a plan whose points are set to another method (1 or 2), bin size
- * and subproblem cap by re-sorting the stored points -- results do not change,
- * only the schedule.  autotune times the plan's spread (type 1) or interp
- * (type 2) stage under the nine layout classes (0-2: method 1 with small,
- * medium, large bins; 3-8: method 2 with those bins x subproblem cap 256 or
- * 1024; bins 1D 256/1024/4096, 2D 16^2/32^2/64^2, 3D 8x8x8/16x16x2/16x16x4)
- * on the plan's own points, keeps the fastest, and reports the chosen entry
- * first followed by the nine classes in order (ms = -2: not runnable). */
+ * switches a plan whose points are set to another method, bin size and
+ * subproblem cap by re-sorting the stored points -- results do not change,
+ * only the schedule.  Methods: 1 (NU-point driven), 2 (subproblems), 5
+ * (type 1 only: method 2 over points sorted by cell inside their bin, with
+ * runs of points on one cell accumulated in registers -- the cell-run
+ * spread; at most 512 taps per point and 2^24 (bin, cell) keys).
+ * autotune times the plan's spread (type 1) or interp (type 2) stage under
+ * the twelve layout classes (0-2: method 1 with small, medium, large bins;
+ * 3-8: method 2 with those bins x subproblem cap 256 or 1024; 9-11: method 5
+ * with those bins, cap 1024; bins 1D 256/1024/4096, 2D 16^2/32^2/64^2, 3D
+ * 8x8x8/16x16x2/16x16x4) on the plan's own points, keeps the fastest, and
+ * reports the chosen entry first followed by the twelve classes in order
+ * (ms = -2: not runnable). */
 typedef struct cufinufft_tune_entry {
   int method, binsizex, binsizey, binsizez, maxsubprobsize;
   float ms;
@@ -152,7 +158,7 @@ int cufinufftf_autotune(cufinufftf_plan plan, cufinufft_tune_entry* entries, int
  * 11 log2(max / mean count), 12 log2(mean count of occupied bins),
  * 13 log2(participation ratio nbins * sum c^2 / (sum c)^2).
  * The network maps standardised features to the predicted log2 time ratio
- * of each of the nine layout classes (see autotune); its parameters are one
+ * of each of the twelve layout classes (see autotune); its parameters are one
  * flat FP32 array of CUFINUFFT_MLP_PARAMS floats,
  *   W1[H][F], b1[H], W2[H][H], b2[H], W3[K][H], b3[K].
  * mlp_forward: X [B][F] -> Y [B][K]; work holds 2*B*H floats.
@@ -162,14 +168,14 @@ int cufinufftf_autotune(cufinufftf_plan plan, cufinufft_tune_entry* entries, int
  * All pointers are device pointers; work is queued on `stream`. */
 #define CUFINUFFT_MLP_FEATURES 14
 #define CUFINUFFT_MLP_HIDDEN 32
-#define CUFINUFFT_MLP_CLASSES 9
+#define CUFINUFFT_MLP_CLASSES 12
 #define CUFINUFFT_MLP_PARAMS                                                             \
   (CUFINUFFT_MLP_HIDDEN * CUFINUFFT_MLP_FEATURES + CUFINUFFT_MLP_HIDDEN +                 \
    CUFINUFFT_MLP_HIDDEN * CUFINUFFT_MLP_HIDDEN + CUFINUFFT_MLP_HIDDEN +                   \
    CUFINUFFT_MLP_CLASSES * CUFINUFFT_MLP_HIDDEN + CUFINUFFT_MLP_CLASSES)
 int cufinufft_features(cufinufft_plan plan, float* features);
 int cufinufftf_features(cufinufftf_plan plan, float* features);
-/* Switch a plan with points set to layout class cls (0-8, see autotune). */
+/* Switch a plan with points set to layout class cls (0-11, see autotune). */
 int cufinufft_set_layout_class(cufinufft_plan plan, int cls);
 int cufinufftf_set_layout_class(cufinufftf_plan plan, int cls);
 int cufinufft_mlp_forward(const float* params, const float* X, int B, float* Y, float* work,

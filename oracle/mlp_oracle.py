@@ -5,7 +5,7 @@ kernels (cufinufft_gb300/csrc/mlp.cu) and for the committed selector weights.
 The network has no counterpart in the reference (cuFINUFFT v1.3 picks its
 method from opts.gpu_method alone, src/cufinufft.cu:103-112 of the reference);
 it is checked here against its own mathematical definition:
-  features F=14 -> H=32 (ReLU) -> H=32 (ReLU) -> K=9,
+  features F=14 -> H=32 (ReLU) -> H=32 (ReLU) -> K=12,
   params = [W1[H][F], b1[H], W2[H][H], b2[H], W3[K][H], b3[K]],
   L = sum m (y - t)^2 / sum m.
 """
@@ -15,7 +15,7 @@ import re
 
 import numpy as np
 
-F, H, K = 14, 32, 9
+F, H, K = 14, 32, 12
 SHAPES = [("W1", (H, F)), ("b1", (H,)), ("W2", (H, H)), ("b2", (H,)), ("W3", (K, H)), ("b3", (K,))]
 NPARAM = sum(int(np.prod(s)) for _, s in SHAPES)
 

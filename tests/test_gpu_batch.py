@@ -122,3 +122,32 @@ def test_batch_rejects_mixed_plans():
     c = cufinufft(1, (16, 16), eps=1e-5, dtype=np.float32)
     with pytest.raises(RuntimeError):
         cufinufft_batch([a, c])           # c has no points yet
+
+
+def test_batch_with_cell_run_plans():
+    """Plans switched to the cell-run layout (method 5) run in the batch
+    through the multi-plan cell-run kernel and give their own results."""
+    import torch
+
+    from cufinufft_gb300 import cufinufft_batch
+    plans, inputs = _plans(1, True, 2, seed=91, nplans=6)
+    for i, p in enumerate(plans):
+        if i % 2 == 0 and inputs[i][1] > 0:
+            p.set_layout(5, (16, 16), 1024)
+            assert p.info()["cell_order"] == 1
+    refs = [_run_single(p, 1, *inp[:3], inp[4]) for p, inp in zip(plans, inputs)]
+    batch = cufinufft_batch(plans)
+    cs, fks = [], []
+    for (modes, M, ntr, pts, data) in inputs:
+        d = torch.from_numpy(data).cuda()
+        cs.append(d)
+        fks.append(torch.zeros((ntr,) + modes[::-1], dtype=d.dtype, device="cuda"))
+    batch.execute(cs, fks)
+    torch.cuda.synchronize()
+    for i, (o, r) in enumerate(zip(fks, refs)):
+        o = o.cpu().numpy()
+        if np.linalg.norm(r) == 0:
+            assert np.all(o == 0)
+            continue
+        err = np.linalg.norm(o.ravel() - r.ravel()) / np.linalg.norm(r.ravel())
+        assert err < 2e-6, (i, err)
