@@ -612,6 +612,7 @@ static int bank_order(Plan<T>* p, int method, const int bs[3], int nbins, BankOr
     o->cell_order = 1;
     o->cls_start = p->cls_start;
     o->sparse_count = p->sparse_count;
+    o->dense_min = dense_run(p->dim);
     return 0;
   }
   // only the one-thread-per-point tile kernels gain: interpolation by default,
@@ -679,7 +680,7 @@ static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
     CFG_CUDA(launch_bin_count<T>(a, p->stream));
     CFG_CUDA(launch_scan(p->count, p->start, p->nbins, 0, 1, p->scan_tmp, p->stream));
     if (a.bank.cell_order)
-      CFG_CUDA(launch_scan(p->cls_count, p->cls_start, p->nbins * a.bank.ncls, 2, kDenseRun, p->cls_tmp,
+      CFG_CUDA(launch_scan(p->cls_count, p->cls_start, p->nbins * a.bank.ncls, 2, dense_run(p->dim), p->cls_tmp,
                            p->stream));
     CFG_CUDA(launch_permute<T>(a, p->stream));
     if (p->method == 2) {
@@ -900,6 +901,7 @@ static int build_subproblems(Plan<T>* p) {
     c.ncls = 1;
     for (int k = 0; k < p->dim; ++k) c.ncls *= p->bs[k];
     c.nsub = nsub;
+    c.dense_min = dense_run(p->dim);
     c.dense = p->sub_dense;
     CFG_CUDA(launch_classify_subproblems(c, p->stream));
   }
@@ -975,7 +977,7 @@ static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub)
     CFG_CUDA(launch_rebin_count<T>(a, p->stream));
     CFG_CUDA(launch_scan(p->count, p->start, (int)nbins, 0, 1, p->scan_tmp, p->stream));
     if (a.bank.cell_order)
-      CFG_CUDA(launch_scan(p->cls_count, p->cls_start, (int)nbins * a.bank.ncls, 2, kDenseRun, p->cls_tmp,
+      CFG_CUDA(launch_scan(p->cls_count, p->cls_start, (int)nbins * a.bank.ncls, 2, dense_run(p->dim), p->cls_tmp,
                            p->stream));
     CFG_CUDA(launch_rebin_permute<T>(a, p->stream));
     CFG_CUDA(cudaStreamSynchronize(p->stream));

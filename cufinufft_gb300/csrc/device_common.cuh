@@ -152,6 +152,31 @@ __device__ __forceinline__ T kernel_tap(T d, int j, const KernelCoeffs<T>& kc) {
   return es_eval(kc.c * x * x, kc);
 }
 
+// ---- packed FP32 pairs (sm_100+) -----------------------------------------
+// c + a * b on both halves of a float2 in one instruction; each half is the
+// IEEE fma of that half, so results equal two scalar fmaf calls.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)),
+        "l"(*reinterpret_cast<unsigned long long*>(&c)));
+  return *reinterpret_cast<float2*>(&d);
+}
+
+// ---- asynchronous global -> shared copies (sm_80+) ------------------------
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // ---- atomics ---------------------------------------------------------------
 // Complex add into global memory: one vector reduction for FP32 (sm_90+),
 // two scalar reductions for FP64.

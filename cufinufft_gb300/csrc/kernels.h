@@ -25,10 +25,12 @@ cudaError_t interp_dim(int method, int ns, const SpreadArgs<T>& a, cudaStream_t 
 //
 // cell_order = 1 instead groups a bin's points for the cell-run spread (class
 // = cell index inside the bin, ncls = cells per bin): points on cells holding
-// at least 32 points first, sorted by cell, then the others in arbitrary
+// at least dense_min points first, sorted by cell, then the others in arbitrary
 // order; cls_start is the exclusive scan of those dense counts over all
 // (bin, cell) keys, sparse_count a per-bin counter for the others.
-constexpr int kDenseRun = 32;  // points on one cell that make it dense (one warp chunk)
+// Points on one cell that make it dense for the cell-run spread: a run must
+// amortise the flush of ns^d tap sums, 36 in 2D at ns = 6, 343 in 3D at 7.
+constexpr int dense_run(int dim) { return dim == 3 ? 16 : 8; }
 
 struct BankOrder {
   int* cls_count;   // [nbins * ncls], zeroed before counting
@@ -37,6 +39,7 @@ struct BankOrder {
   int cell_order;
   const int* cls_start;  // [nbins * ncls + 1] (cell_order only)
   int* sparse_count;     // [nbins], zeroed before permuting (cell_order only)
+  int dense_min;         // dense_run(dim) (cell_order only)
 };
 
 template <typename T> struct PlaceArgs {
@@ -100,7 +103,7 @@ struct SubClassArgs {
   const int* i0[3];
   const int* cls_count;
   int bs[3];
-  int dim, maxsub, ncls, nsub;
+  int dim, maxsub, ncls, nsub, dense_min;
   unsigned char* dense;
 };
 cudaError_t launch_classify_subproblems(const SubClassArgs& a, cudaStream_t s);

@@ -70,7 +70,7 @@ __device__ __forceinline__ int agg_rank(unsigned act, int key, int* counter) {
 }
 
 // Cell order (BankOrder::cell_order): a bin's points on dense cells (at least
-// kDenseRun points) come first, sorted by cell -- cls_start is the exclusive
+// dense_min points) come first, sorted by cell -- cls_start is the exclusive
 // scan of the dense cells' counts only -- then the bin's other points in
 // arbitrary order, ranked by the per-bin counter sparse_count.  r is the
 // point's rank inside its cell.  Called by the lanes in act together.
@@ -78,7 +78,7 @@ __device__ __forceinline__ int cell_position(const BankOrder& o, const int* star
                                              int c, int r) {
   const long long k0 = (long long)b * o.ncls;
   const int bin0 = o.cls_start[k0];
-  const bool dense = o.cls_count[k0 + c] >= kDenseRun;
+  const bool dense = o.cls_count[k0 + c] >= o.dense_min;
   const unsigned sparse_lanes = __ballot_sync(act, !dense);
   if (dense) return start[b] + (o.cls_start[k0 + c] - bin0) + r;
   const int sr = agg_rank(sparse_lanes, b, o.sparse_count + b);
@@ -431,7 +431,7 @@ __global__ void k_classify_subproblems(SubClassArgs a) {
     const int ly = a.dim > 1 ? a.i0[1][p0] % a.bs[1] : 0;
     const int lz = a.dim > 2 ? a.i0[2][p0] % a.bs[2] : 0;
     const int c = lx + a.bs[0] * (ly + a.bs[1] * lz);
-    a.dense[sidx] = a.cls_count[(long long)b * a.ncls + c] >= kDenseRun ? 1 : 0;
+    a.dense[sidx] = a.cls_count[(long long)b * a.ncls + c] >= a.dense_min ? 1 : 0;
   }
 }
 

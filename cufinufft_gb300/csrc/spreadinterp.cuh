@@ -69,9 +69,12 @@ __device__ __forceinline__ void tile_load(cplx_t<T>* tile, const cplx_t<T>* grid
     for (int ix = lane; ix < st.TX; ix += 32) {
       int gx = st.ox + ix;
       while (gx >= g.nf[0]) gx -= g.nf[0];
-      dst[ix] = __ldg(src + gx);
+      // asynchronous copy: no register round trip, many cells in flight
+      if constexpr (sizeof(T) == 4) cp_async8(dst + ix, src + gx);
+      else cp_async16(dst + ix, src + gx);
     }
   }
+  cp_async_wait();  // this thread's copies have landed; the caller syncs the block
 }
 
 // Add the tile back into the fine grid with vector reductions, skipping the
@@ -274,31 +277,56 @@ k_interp_sm(SpreadArgs<T> a) {
     if (DIM > 1) { ly = a.pts.i0[1][p] - st.oy; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
     T d3 = T(0);
     if (DIM > 2) { lz = a.pts.i0[2][p] - st.oz; d3 = a.pts.d[2][p]; }
-    T ar = T(0), ai = T(0);
-#pragma unroll 1
-    for (int dz = 0; dz < NZ; ++dz) {
-      const T kz = DIM > 2 ? kernel_tap<T, NS, HD>(d3, dz, a.kc) : T(1);
-      const C* plane = tile + ((lz + dz) * st.TY + ly) * st.TX + lx;
-#pragma unroll
-      for (int dy = 0; dy < NY; ++dy) {
-        const C* row = plane + dy * st.TX;
-        T rr = T(0), ri = T(0);
-#pragma unroll
-        for (int dx = 0; dx < NS; ++dx) {
-          const C g = row[dx];
-          rr = fma_rn(g.x, k1[dx], rr);
-          ri = fma_rn(g.y, k1[dx], ri);
-        }
-        T kyz = T(1);
-        if (DIM > 1) kyz = k2[dy];
-        if (DIM > 2) kyz *= kz;
-        ar = fma_rn(rr, kyz, ar);
-        ai = fma_rn(ri, kyz, ai);
-      }
-    }
     C out;
-    out.x = ar;
-    out.y = ai;
+    if constexpr (sizeof(T) == 4) {
+      // packed pairs: one fma.rn.f32x2 per complex tap (same IEEE fmas)
+      float2 k1p[NS];
+#pragma unroll
+      for (int dx = 0; dx < NS; ++dx) k1p[dx] = make_float2(k1[dx], k1[dx]);
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 1
+      for (int dz = 0; dz < NZ; ++dz) {
+        const T kz = DIM > 2 ? kernel_tap<T, NS, HD>(d3, dz, a.kc) : T(1);
+        const C* plane = tile + ((lz + dz) * st.TY + ly) * st.TX + lx;
+#pragma unroll
+        for (int dy = 0; dy < NY; ++dy) {
+          const C* row = plane + dy * st.TX;
+          float2 r = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int dx = 0; dx < NS; ++dx) r = fma2(row[dx], k1p[dx], r);
+          T kyz = T(1);
+          if (DIM > 1) kyz = k2[dy];
+          if (DIM > 2) kyz *= kz;
+          acc = fma2(r, make_float2(kyz, kyz), acc);
+        }
+      }
+      out = acc;
+    } else {
+      T ar = T(0), ai = T(0);
+#pragma unroll 1
+      for (int dz = 0; dz < NZ; ++dz) {
+        const T kz = DIM > 2 ? kernel_tap<T, NS, HD>(d3, dz, a.kc) : T(1);
+        const C* plane = tile + ((lz + dz) * st.TY + ly) * st.TX + lx;
+#pragma unroll
+        for (int dy = 0; dy < NY; ++dy) {
+          const C* row = plane + dy * st.TX;
+          T rr = T(0), ri = T(0);
+#pragma unroll
+          for (int dx = 0; dx < NS; ++dx) {
+            const C g = row[dx];
+            rr = fma_rn(g.x, k1[dx], rr);
+            ri = fma_rn(g.y, k1[dx], ri);
+          }
+          T kyz = T(1);
+          if (DIM > 1) kyz = k2[dy];
+          if (DIM > 2) kyz *= kz;
+          ar = fma_rn(rr, kyz, ar);
+          ai = fma_rn(ri, kyz, ai);
+        }
+      }
+      out.x = ar;
+      out.y = ai;
+    }
     a.c_out[(size_t)t * a.M + a.pts.idx[p]] = out;
   }
 }
@@ -550,11 +578,11 @@ __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, 
   const int beg = warp * S;
   const int end = min(st.np, beg + S);
   // The cursor follows the runs: a window of 32 points whose leading run
-  // (points on the window's first cell) has at least kMinRun points is
+  // (points on the window's first cell) has at least dense_run(DIM) points is
   // accumulated -- the run's first n <= 32 points -- and the cursor moves by
   // n, so the next window starts at a run boundary; any other window is
   // spread point by point and the cursor moves by 32.
-  constexpr int kMinRun = 16;
+  constexpr int kMinRun = dense_run(DIM);
   int cs = beg;
   while (cs < end) {  // warp-uniform
     const int ql = cs + lane;
