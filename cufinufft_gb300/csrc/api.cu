@@ -94,6 +94,8 @@ template <typename T> static void release(Plan<T>* p) {
   p->have_fft = p->have_fft_rem = false;
   cudaFree(p->fw);
   p->fw = nullptr;
+  cudaFree(p->fw2);
+  p->fw2 = nullptr;
   for (int k = 0; k < 3; ++k) {
     cudaFree(p->fac[k]);
     p->fac[k] = nullptr;
@@ -505,6 +507,12 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
     e = make_line_fft(p);
     if (e) return e;
   } else {
+    if (type == 2) {
+      // out-of-place FFT: fw holds only the amplified modes over padding
+      // zeroed once here, the FFT writes fw2, interpolation reads fw2
+      CFG_CUDA(cudaMalloc(&p->fw2, sizeof(cplx_t<T>) * (size_t)Nf * p->maxbatch));
+      CFG_CUDA(cudaMemsetAsync(p->fw, 0, sizeof(cplx_t<T>) * (size_t)Nf * p->maxbatch, p->stream));
+    }
     e = make_fft(p, p->maxbatch, &p->fft);
     if (e) return e;
     p->have_fft = true;
@@ -795,13 +803,13 @@ static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
         }
         mark(p, ev[2]);
       } else {
-        CFG_CUDA(launch_amplify<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
-                                   p->fac[1], p->fac[2], B, p->stream));
+        CFG_CUDA(launch_amplify_modes<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
+                                         p->fac[1], p->fac[2], B, p->stream));
         mark(p, ev[1]);
-        CFG_CUFFT(fft_exec(h, p->fw, p->iflag));
+        CFG_CUFFT(fft_exec(h, p->fw, p->fw2, p->iflag));
         mark(p, ev[2]);
       }
-      a.fw_in = p->fw;
+      a.fw_in = p->fw2 ? p->fw2 : p->fw;
       a.c_out = c + (size_t)b0 * p->M;
       CFG_CUDA(run_interp(p, a));
     }
@@ -1029,7 +1037,7 @@ static int time_stage(Plan<T>* p, cplx_t<T>* scratch, int reps, float* ms) {
       a.fw = p->fw;
       CFG_CUDA(run_spread(p, a));
     } else {
-      a.fw_in = p->fw;
+      a.fw_in = p->fw2 ? p->fw2 : p->fw;
       a.c_out = scratch;
       CFG_CUDA(run_interp(p, a));
     }
@@ -1102,7 +1110,8 @@ static int autotune_impl(Plan<T>* p, cufinufft_tune_entry* out, int max_out, int
   // nonzero synthetic strengths/values (a zero tile would be skipped)
   CFG_CUDA(cudaMemsetAsync(scratch, 0x3f, sizeof(cplx_t<T>) * (size_t)p->M * p->maxbatch, p->stream));
   if (p->type == 2)
-    CFG_CUDA(cudaMemsetAsync(p->fw, 0x3f, sizeof(cplx_t<T>) * (size_t)grid_cells(p) * p->maxbatch,
+    CFG_CUDA(cudaMemsetAsync(p->fw2 ? p->fw2 : p->fw, 0x3f,
+                             sizeof(cplx_t<T>) * (size_t)grid_cells(p) * p->maxbatch,
                              p->stream));
   int best = -1;
   for (size_t i = 0; i < cand.size(); ++i) {

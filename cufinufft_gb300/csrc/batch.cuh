@@ -280,7 +280,7 @@ k_batch_spread_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
     const int t = (int)(local / P.bins.nsub);
     const int sub = (int)(local - (long long)t * P.bins.nsub);
     if (P.sub_dense && P.sub_dense[sub]) continue;  // cell-run layout: k_batch_spread_run
-    const SubTile st = sub_tile<DIM, NS>(P.bins, sub);
+    const SubTile st = sub_tile_block<DIM, NS, true>(P.bins, sub);
     T* re = reinterpret_cast<T*>(smem_raw);  // real plane, then imaginary plane
     T* im = re + st.ntile;
     __syncthreads();  // the previous task's flush is done with the tile
@@ -342,7 +342,7 @@ k_batch_spread_run(const BatchDesc<T>* D, int nplans, long long nblocks) {
     const int t = (int)(local / P.bins.nsub);
     const int sub = (int)(local - (long long)t * P.bins.nsub);
     if (!(P.sub_dense && P.sub_dense[sub])) continue;
-    const SubTile st = sub_tile<DIM, NS>(P.bins, sub);
+    const SubTile st = sub_tile_block<DIM, NS, true>(P.bins, sub);
     T* re = reinterpret_cast<T*>(smem_raw);
     T* im = re + st.ntile;
     __syncthreads();  // the previous task's flush is done with the tile
@@ -387,7 +387,7 @@ k_batch_interp_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
     const long long local = task - P.blk0;
     const int t = (int)(local / P.bins.nsub);
     const int sub = (int)(local - (long long)t * P.bins.nsub);
-    const SubTile st = sub_tile<DIM, NS>(P.bins, sub);
+    const SubTile st = sub_tile_block<DIM, NS, true>(P.bins, sub);
     GridGeom gg;
     gg.nf[0] = P.nf[0];
     gg.nf[1] = P.nf[1];

@@ -11,8 +11,11 @@
 // deconvolve / amplify restate Deconvolve_{1,2,3}d / Amplify_{1,2,3}d
 // (src/deconvolve_wrapper.cu:14-121): mode k_d in -N_d/2..(N_d-1)/2 lives at
 // fine-grid index k_d mod nf_d.  Both kernels handle the whole batch in one
-// launch, and amplify writes every fine-grid cell (zero or mode) in one pass,
-// replacing the reference's full cudaMemset plus scatter.
+// launch.  Amplify writes only the mode cells: the plan zeroes the padding
+// of its grid once and runs the type-2 FFT out of place, so the padding
+// stays zero (the reference clears the whole grid on every execute).
+#include <algorithm>
+
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -93,81 +96,6 @@ k_deconvolve(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, const c
   }
 }
 
-// One block row per fine-grid row (w2, w3); each thread writes two adjacent
-// cells (one 16-byte store in FP32).  Rows outside the mode band and cells
-// between the positive and negative x-modes are 0.
-template <typename T>
-__device__ __forceinline__ cplx_t<T> amp_cell(int w1, int nf0, int N0, const cplx_t<T>* src,
-                                              const T* __restrict__ fac0, T f23) {
-  cplx_t<T> o;
-  const int k1 = w1 <= (N0 - 1) / 2 ? w1 : (w1 >= nf0 - N0 / 2 ? w1 - nf0 : nf0);
-  if (k1 == nf0) {
-    o.x = T(0);
-    o.y = T(0);
-  } else {
-    const int i1 = k1 + N0 / 2;
-    const T f = fac0[i1] * f23;
-    const cplx_t<T> v = src[i1];
-    o.x = v.x * f;
-    o.y = v.y * f;
-  }
-  return o;
-}
-
-__device__ __forceinline__ void store_pair(float2* dst, float2 a, float2 b) {
-  *reinterpret_cast<float4*>(dst) = make_float4(a.x, a.y, b.x, b.y);
-}
-__device__ __forceinline__ void store_pair(double2* dst, double2 a, double2 b) {
-  dst[0] = a;
-  dst[1] = b;
-}
-
-template <typename T>
-__global__ void __launch_bounds__(256)
-k_amplify(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, cplx_t<T>* __restrict__ fw,
-          const cplx_t<T>* __restrict__ fk, const T* __restrict__ fac0, const T* __restrict__ fac1,
-          const T* __restrict__ fac2, int ntr) {
-  using C = cplx_t<T>;
-  const long long Nf = (long long)nf0 * nf1 * nf2;
-  const long long Nm = (long long)N0 * N1 * N2;
-  const int nrows = nf1 * nf2;
-  const int npairs = nf0 / 2;  // nf0 is even
-  for (int r = blockIdx.x; r < nrows * ntr; r += gridDim.x) {
-    const int t = r / nrows;
-    const int rr = r - t * nrows;
-    const int w2 = rr % nf1, w3 = rr / nf1;
-    int i2 = 0, i3 = 0;
-    bool live = true;
-    if (dim > 1) {
-      const int k2 = w2 <= (N1 - 1) / 2 ? w2 : (w2 >= nf1 - N1 / 2 ? w2 - nf1 : nf1);
-      live = live && k2 != nf1;
-      i2 = k2 + N1 / 2;
-    }
-    if (dim > 2) {
-      const int k3 = w3 <= (N2 - 1) / 2 ? w3 : (w3 >= nf2 - N2 / 2 ? w3 - nf2 : nf2);
-      live = live && k3 != nf2;
-      i3 = k3 + N2 / 2;
-    }
-    C* dst = fw + (size_t)t * Nf + ((size_t)w3 * nf1 + w2) * nf0;
-    if (!live) {
-      C z;
-      z.x = T(0);
-      z.y = T(0);
-      for (int q = threadIdx.x; q < npairs; q += blockDim.x) store_pair(dst + 2 * q, z, z);
-      continue;
-    }
-    T f23 = T(1);
-    if (dim > 1) f23 = fac1[i2];
-    if (dim > 2) f23 *= fac2[i3];
-    const C* src = fk + (size_t)t * Nm + ((size_t)i3 * N1 + i2) * N0;
-    for (int q = threadIdx.x; q < npairs; q += blockDim.x) {
-      const C a = amp_cell<T>(2 * q, nf0, N0, src, fac0, f23);
-      const C b = amp_cell<T>(2 * q + 1, nf0, N0, src, fac0, f23);
-      store_pair(dst + 2 * q, a, b);
-    }
-  }
-}
-
 static int row_grid(long long rows) {
   long long cap = 152LL * 16;
   return (int)(rows < cap ? (rows < 1 ? 1 : rows) : cap);
@@ -183,15 +111,59 @@ cudaError_t launch_deconvolve(int dim, const int nf[3], const int N[3], const cp
   return cudaGetLastError();
 }
 
+// Type-2 amplification into a grid whose padding is already zero (the FFT
+// then runs out of place): only the mode cells are written, one block row per
+// (k2, k3) mode row, threads over k1 -- the mirror of k_deconvolve.
 template <typename T>
-cudaError_t launch_amplify(int dim, const int nf[3], const int N[3], cplx_t<T>* fw,
-                           const cplx_t<T>* fk, const T* fac0, const T* fac1, const T* fac2, int ntr,
-                           cudaStream_t s) {
-  long long rows = (long long)nf[1] * nf[2] * ntr;
-  k_amplify<T><<<row_grid(rows), 256, 0, s>>>(dim, nf[0], nf[1], nf[2], N[0], N[1], N[2], fw, fk,
-                                              fac0, fac1, fac2, ntr);
+__global__ void __launch_bounds__(256)
+k_amplify_modes(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, cplx_t<T>* __restrict__ fw,
+                const cplx_t<T>* __restrict__ fk, const T* __restrict__ fac0, const T* __restrict__ fac1,
+                const T* __restrict__ fac2, int ntr) {
+  using C = cplx_t<T>;
+  const long long Nf = (long long)nf0 * nf1 * nf2;
+  const long long Nm = (long long)N0 * N1 * N2;
+  const int nrows = N1 * N2;
+  for (int r = blockIdx.x; r < nrows * ntr; r += gridDim.x) {
+    const int t = r / nrows;
+    const int rr = r - t * nrows;
+    const int i2 = rr % N1, i3 = rr / N1;
+    const int k2 = i2 - N1 / 2, k3 = i3 - N2 / 2;
+    const int w2 = k2 >= 0 ? k2 : nf1 + k2;
+    const int w3 = k3 >= 0 ? k3 : nf2 + k3;
+    T f23 = T(1);
+    if (dim > 1) f23 = fac1[i2];
+    if (dim > 2) f23 *= fac2[i3];
+    C* dst = fw + (size_t)t * Nf + ((size_t)w3 * nf1 + w2) * nf0;
+    const C* src = fk + (size_t)t * Nm + ((size_t)i3 * N1 + i2) * N0;
+    for (int i1 = threadIdx.x; i1 < N0; i1 += blockDim.x) {
+      const int k1 = i1 - N0 / 2;
+      const int w1 = k1 >= 0 ? k1 : nf0 + k1;
+      const T f = fac0[i1] * f23;
+      const C v = src[i1];
+      C o;
+      o.x = v.x * f;
+      o.y = v.y * f;
+      dst[w1] = o;
+    }
+  }
+}
+
+template <typename T>
+cudaError_t launch_amplify_modes(int dim, const int nf[3], const int N[3], cplx_t<T>* fw,
+                                 const cplx_t<T>* fk, const T* fac0, const T* fac1, const T* fac2,
+                                 int ntr, cudaStream_t s) {
+  const long long rows = (long long)N[1] * N[2] * ntr;
+  const int grid = (int)std::min<long long>(std::max<long long>(rows, 1), 152LL * 32);
+  k_amplify_modes<T><<<grid, 256, 0, s>>>(dim, nf[0], nf[1], nf[2], N[0], N[1], N[2], fw, fk, fac0,
+                                          fac1, fac2, ntr);
   return cudaGetLastError();
 }
+template cudaError_t launch_amplify_modes<float>(int, const int*, const int*, cplx_t<float>*,
+                                                 const cplx_t<float>*, const float*, const float*,
+                                                 const float*, int, cudaStream_t);
+template cudaError_t launch_amplify_modes<double>(int, const int*, const int*, cplx_t<double>*,
+                                                  const cplx_t<double>*, const double*,
+                                                  const double*, const double*, int, cudaStream_t);
 
 template cudaError_t launch_fseries<float>(const FseriesNodes&, int, const int*, const int*, float*,
                                            float*, float*, cudaStream_t);
@@ -203,11 +175,5 @@ template cudaError_t launch_deconvolve<float>(int, const int*, const int*, const
 template cudaError_t launch_deconvolve<double>(int, const int*, const int*, const double2*, double2*,
                                                const double*, const double*, const double*, int,
                                                cudaStream_t);
-template cudaError_t launch_amplify<float>(int, const int*, const int*, float2*, const float2*,
-                                           const float*, const float*, const float*, int,
-                                           cudaStream_t);
-template cudaError_t launch_amplify<double>(int, const int*, const int*, double2*, const double2*,
-                                            const double*, const double*, const double*, int,
-                                            cudaStream_t);
 
 }  // namespace cfg

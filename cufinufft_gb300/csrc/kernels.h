@@ -127,11 +127,9 @@ cudaError_t launch_deconvolve(int dim, const int nf[3], const int N[3], const cp
                               int ntr, cudaStream_t s);
 // Type 2: fw[t] = 0 except the mode cells, fw[t][mode m] = fk[t][m] * prod fac.
 template <typename T>
-cudaError_t launch_amplify(int dim, const int nf[3], const int N[3], cplx_t<T>* fw,
-                           const cplx_t<T>* fk, const T* fac0, const T* fac1, const T* fac2,
-                           int ntr, cudaStream_t s);
-
-
+cudaError_t launch_amplify_modes(int dim, const int nf[3], const int N[3], cplx_t<T>* fw,
+                                 const cplx_t<T>* fk, const T* fac0, const T* fac1, const T* fac2,
+                                 int ntr, cudaStream_t s);
 // Pruned line FFTs (fftpass.cu).  A pass transforms nlines lines of length
 // L; line l has indices la = l % A and lb = l / A.  Each side (input, output)
 // maps a line and a position to memory:

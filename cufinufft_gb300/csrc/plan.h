@@ -44,6 +44,7 @@ template <typename T> struct Plan {
   std::vector<int> rad[3];
   int rem = 0;
   C* fw = nullptr;
+  C* fw2 = nullptr;  // type 2 with cuFFT: FFT output (fw keeps zero padding between executes)
   T* fac[3] = {nullptr, nullptr, nullptr};
   std::vector<T> horner;  // fitted kernel polynomials (kerevalmeth 1), [k][j]
   T* horner_d = nullptr;  // device copy of the same
@@ -120,6 +121,12 @@ inline cufftResult fft_exec(cufftHandle h, float2* data, int dir) {
 }
 inline cufftResult fft_exec(cufftHandle h, double2* data, int dir) {
   return cufftExecZ2Z(h, (cufftDoubleComplex*)data, (cufftDoubleComplex*)data, dir);
+}
+inline cufftResult fft_exec(cufftHandle h, float2* in, float2* out, int dir) {
+  return cufftExecC2C(h, (cufftComplex*)in, (cufftComplex*)out, dir);
+}
+inline cufftResult fft_exec(cufftHandle h, double2* in, double2* out, int dir) {
+  return cufftExecZ2Z(h, (cufftDoubleComplex*)in, (cufftDoubleComplex*)out, dir);
 }
 
 template <typename T> inline long long grid_cells(const Plan<T>* p) {

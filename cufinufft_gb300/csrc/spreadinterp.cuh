@@ -52,23 +52,55 @@ __device__ __forceinline__ SubTile sub_tile(const BinTables& bt, int sub) {
   return s;
 }
 
+// sub_tile computed once per block (three integer divisions) and shared
+// through shared memory; PERSISTENT blocks (several subproblems each) first
+// wait until every thread is done with the previous one.
+template <int DIM, int NS, bool PERSISTENT = false>
+__device__ __forceinline__ SubTile sub_tile_block(const BinTables& bt, int sub) {
+  __shared__ SubTile s_tile;
+  if (PERSISTENT) __syncthreads();
+  if (threadIdx.x == 0) s_tile = sub_tile<DIM, NS>(bt, sub);
+  __syncthreads();
+  return s_tile;
+}
+
+// v wrapped into [0, n) for 0 <= v < 3n: two conditional subtractions.
+__device__ __forceinline__ int wrap3(int v, int n) {
+  v -= v >= n ? n : 0;
+  v -= v >= n ? n : 0;
+  return v;
+}
+
+// Tile rows (iy, iz) visited by one warp: rows warp, warp + nwarps, ...,
+// advanced without divisions.
+struct TileRows {
+  int iy, iz;
+  __device__ __forceinline__ TileRows(int r, int TY) : iy(r % TY), iz(r / TY) {}
+  __device__ __forceinline__ void next(int step, int TY) {
+    iy += step;
+    while (iy >= TY) {
+      iy -= TY;
+      ++iz;
+    }
+  }
+};
+
 // Copy the subproblem's padded tile from the fine grid (periodic wrap) into
-// shared memory: one warp per tile row, lanes along x.
+// shared memory: one warp per tile row, lanes along x.  Tile coordinates
+// stay below 3 nf (bins within the grid, halo ns - 1 <= nf / 2), so two
+// conditional subtractions wrap them.
 template <typename T>
 __device__ __forceinline__ void tile_load(cplx_t<T>* tile, const cplx_t<T>* grid, const SubTile& st,
                                           const GridGeom& g) {
   const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
   const int rows = st.TY * st.TZ;
-  for (int r = threadIdx.x >> 5; r < rows; r += nwb) {
-    const int iy = r % st.TY, iz = r / st.TY;
-    int gy = st.oy + iy, gz = st.oz + iz;
-    while (gy >= g.nf[1]) gy -= g.nf[1];
-    while (gz >= g.nf[2]) gz -= g.nf[2];
+  TileRows rw(threadIdx.x >> 5, st.TY);
+  for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
+    const int gy = wrap3(st.oy + rw.iy, g.nf[1]), gz = wrap3(st.oz + rw.iz, g.nf[2]);
     const cplx_t<T>* src = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
     cplx_t<T>* dst = tile + r * st.TX;
     for (int ix = lane; ix < st.TX; ix += 32) {
-      int gx = st.ox + ix;
-      while (gx >= g.nf[0]) gx -= g.nf[0];
+      const int gx = wrap3(st.ox + ix, g.nf[0]);
       // asynchronous copy: no register round trip, many cells in flight
       if constexpr (sizeof(T) == 4) cp_async8(dst + ix, src + gx);
       else cp_async16(dst + ix, src + gx);
@@ -84,19 +116,15 @@ __device__ __forceinline__ void tile_flush(const cplx_t<T>* tile, cplx_t<T>* gri
                                            const GridGeom& g) {
   const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
   const int rows = st.TY * st.TZ;
-  for (int r = threadIdx.x >> 5; r < rows; r += nwb) {
-    const int iy = r % st.TY, iz = r / st.TY;
-    int gy = st.oy + iy, gz = st.oz + iz;
-    while (gy >= g.nf[1]) gy -= g.nf[1];
-    while (gz >= g.nf[2]) gz -= g.nf[2];
+  TileRows rw(threadIdx.x >> 5, st.TY);
+  for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
+    const int gy = wrap3(st.oy + rw.iy, g.nf[1]), gz = wrap3(st.oz + rw.iz, g.nf[2]);
     cplx_t<T>* dst = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
     const cplx_t<T>* src = tile + r * st.TX;
     for (int ix = lane; ix < st.TX; ix += 32) {
       const cplx_t<T> v = src[ix];
       if (v.x == T(0) && v.y == T(0)) continue;
-      int gx = st.ox + ix;
-      while (gx >= g.nf[0]) gx -= g.nf[0];
-      red_add(dst + gx, v.x, v.y);
+      red_add(dst + wrap3(st.ox + ix, g.nf[0]), v.x, v.y);
     }
   }
 }
@@ -165,7 +193,7 @@ k_spread_sm(SpreadArgs<T> a) {
   constexpr int NZ = DIM > 2 ? NS : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tile = reinterpret_cast<C*>(smem_raw);
-  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  const SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
   const int t = blockIdx.y;
   tile_zero<T>(tile, st.ntile);
   __syncthreads();
@@ -257,7 +285,7 @@ k_interp_gm(SpreadArgs<T> a) {
 // ---------------------------------------------------------------------------
 // Method 2: shared-memory subproblem interpolation.  grid = (nsub, ntr).
 template <typename T, int DIM, int NS>
-__global__ void __launch_bounds__(kSpreadThreads)
+__global__ void __launch_bounds__(kSpreadThreads, sizeof(T) == 4 ? (NS <= 9 ? 6 : 4) : 1)  // FP32 ns <= 9: 40 regs, 6 blocks/SM
 k_interp_sm(SpreadArgs<T> a) {
   using C = cplx_t<T>;
   constexpr int HD = horner_degree<T>(NS);
@@ -265,7 +293,7 @@ k_interp_sm(SpreadArgs<T> a) {
   constexpr int NZ = DIM > 2 ? NS : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tile = reinterpret_cast<C*>(smem_raw);
-  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  const SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
   const int t = blockIdx.y;
   tile_load<T>(tile, a.fw_in + (size_t)t * a.g.Nf, st, a.g);
   __syncthreads();
@@ -463,18 +491,14 @@ __device__ __forceinline__ void plane_flush(const T* re, const T* im, cplx_t<T>*
                                             const SubTile& st, const GridGeom& g) {
   const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
   const int rows = st.TY * st.TZ;
-  for (int r = threadIdx.x >> 5; r < rows; r += nwb) {
-    const int iy = r % st.TY, iz = r / st.TY;
-    int gy = st.oy + iy, gz = st.oz + iz;
-    while (gy >= g.nf[1]) gy -= g.nf[1];
-    while (gz >= g.nf[2]) gz -= g.nf[2];
+  TileRows rw(threadIdx.x >> 5, st.TY);
+  for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
+    const int gy = wrap3(st.oy + rw.iy, g.nf[1]), gz = wrap3(st.oz + rw.iz, g.nf[2]);
     cplx_t<T>* dst = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
     for (int ix = lane; ix < st.TX; ix += 32) {
       const T vr = re[r * st.TX + ix], vi = im[r * st.TX + ix];
       if (vr == T(0) && vi == T(0)) continue;
-      int gx = st.ox + ix;
-      while (gx >= g.nf[0]) gx -= g.nf[0];
-      red_add(dst + gx, vr, vi);
+      red_add(dst + wrap3(st.ox + ix, g.nf[0]), vr, vi);
     }
   }
 }
@@ -490,7 +514,7 @@ k_spread_sm_wc(SpreadArgs<T> a) {
   constexpr int NZ = DIM > 2 ? NS : 1;
   if (a.sub_dense && a.sub_dense[blockIdx.x]) return;  // cell-run layout: done by k_spread_sm_run
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  const SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
   T* re = reinterpret_cast<T*>(smem_raw);
   T* im = re + st.ntile;
   const int t = blockIdx.y;
@@ -700,7 +724,7 @@ k_spread_sm_run(SpreadArgs<T> a) {
   constexpr int HD = horner_degree<T>(NS);
   if (a.sub_dense && !a.sub_dense[blockIdx.x]) return;  // sparse: done by k_spread_sm_wc
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  const SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
   T* re = reinterpret_cast<T*>(smem_raw);
   T* im = re + st.ntile;
   const int t = blockIdx.y;
@@ -735,7 +759,7 @@ k_interp_sm_wc(SpreadArgs<T> a) {
   constexpr int NZ = DIM > 2 ? NS : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tile = reinterpret_cast<C*>(smem_raw);
-  const SubTile st = sub_tile<DIM, NS>(a.bins, blockIdx.x);
+  const SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
   const int t = blockIdx.y;
   tile_load<T>(tile, a.fw_in + (size_t)t * a.g.Nf, st, a.g);
   __syncthreads();

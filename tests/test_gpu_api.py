@@ -250,3 +250,35 @@ def test_upsampfac_125():
         err = np.linalg.norm(out.ravel() - d) / np.linalg.norm(d)
         assert err < 5 * max(tol, 2e-5 if single else 0), (err, info)
         assert info["nf1"] < 2 * 30
+
+
+def test_type2_padding_stays_zero_across_executes():
+    """Type 2 with cuFFT zeroes the grid padding once and writes only mode
+    cells per execute (out-of-place FFT): results stay right over repeated
+    executes with new coefficients, after autotuning, and with a partial last
+    batch."""
+    import torch
+
+    from cufinufft_gb300 import cufinufft
+    rng = np.random.default_rng(21)
+    modes = (36, 30)
+    M, ntr = 3000, 5
+    pts = NC.points(rng, 2, M, edges=False)
+    for single in (True, False):
+        dt = np.float32 if single else np.float64
+        cdt = np.complex64 if single else np.complex128
+        tol = 1e-5 if single else 1e-10
+        plan = cufinufft(2, modes[::-1], n_trans=ntr, eps=tol, dtype=dt, maxbatchsize=2)
+        plan.set_pts(*[_cuda(p.astype(dt)) for p in pts[::-1]])
+        assert plan.info()["line_fft"] == 0
+        for rep in range(3):
+            fk = NC.coeffs(rng, modes, ntr).astype(cdt)
+            c = torch.zeros((ntr, M), dtype=_cuda(fk).dtype, device="cuda")
+            plan.execute(c, _cuda(fk))
+            out = c.cpu().numpy()
+            ref = NC.oracle_nufft(2, modes, [p.astype(np.float64) for p in pts],
+                                  fk.astype(np.complex128), tol, single, ntr=ntr)
+            err = np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
+            assert err < (2e-5 if single else 1e-10), (single, rep, err)
+            if rep == 0:
+                plan.autotune()
