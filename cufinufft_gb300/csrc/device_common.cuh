@@ -153,16 +153,10 @@ __device__ __forceinline__ T kernel_tap(T d, int j, const KernelCoeffs<T>& kc) {
 }
 
 // ---- packed FP32 pairs (sm_100+) -----------------------------------------
-// c + a * b on both halves of a float2 in one instruction; each half is the
-// IEEE fma of that half, so results equal two scalar fmaf calls.
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
-  unsigned long long d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;"
-      : "=l"(d)
-      : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)),
-        "l"(*reinterpret_cast<unsigned long long*>(&c)));
-  return *reinterpret_cast<float2*>(&d);
-}
+// c + a * b on both halves of a float2 in one instruction (CUDA's
+// __ffma2_rn); each half is the IEEE fma of that half, so results equal two
+// scalar fmaf calls.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
 // ---- asynchronous global -> shared copies (sm_80+) ------------------------
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
