@@ -20,6 +20,11 @@
 //     flush skips cells no point touched.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap and its encoder's types (the encoder is fetched at run time)
+
+#include <cstdlib>
+#include <cstring>
+
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -127,6 +132,95 @@ __device__ __forceinline__ void tile_flush(const cplx_t<T>* tile, cplx_t<T>* gri
       red_add(dst + wrap3(st.ox + ix, g.nf[0]), v.x, v.y);
     }
   }
+}
+
+// ---- TMA tile loads (interpolation) ---------------------------------------
+// The fine grids are described to the copy engine as a (DIM+1)-rank tensor
+// of real components: x runs over 2 nf0 reals, then y, z and the transform
+// index.  A subproblem tile that does not wrap the periodic edge is one box
+// of that tensor ({2 TX, TY, TZ, 1} at (2 ox, oy, oz, t)), moved into shared
+// memory by one tiled bulk copy that one thread issues; the block waits on
+// an mbarrier.  Tiles that wrap keep the per-cell cp.async path.
+
+// Polls of the tile barrier before a thread gives up on the bulk copy and
+// loads its share of the tile itself (the data is the same either way).
+constexpr int kTmaWaitPolls = 1 << 20;
+
+template <int DIM>
+__device__ __forceinline__ bool tile_inside(const SubTile& st, const GridGeom& g) {
+  return st.ox + st.TX <= g.nf[0] && (DIM < 2 || st.oy + st.TY <= g.nf[1]) &&
+         (DIM < 3 || st.oz + st.TZ <= g.nf[2]);
+}
+
+// Shared-memory start of the tile rounded up to 128 bytes (bulk tensor
+// copies want an aligned destination; the launch adds 128 bytes).
+__device__ __forceinline__ unsigned char* smem_align128(unsigned char* p) {
+  return p + ((128u - (smem_u32(p) & 127u)) & 127u);
+}
+
+template <typename T, int DIM>
+__device__ __forceinline__ void tile_load_tma(cplx_t<T>* tile, const CUtensorMap* map, const SubTile& st,
+                                              int t, unsigned long long* bar, const cplx_t<T>* grid,
+                                              const GridGeom& g) {
+  if (threadIdx.x == 0) {
+    mbar_expect_tx(bar, (unsigned)(st.ntile * sizeof(cplx_t<T>)));
+    if constexpr (DIM == 1) tma_load2(tile, map, 2 * st.ox, t, bar);
+    else if constexpr (DIM == 2) tma_load3(tile, map, 2 * st.ox, st.oy, t, bar);
+    else tma_load4(tile, map, 2 * st.ox, st.oy, st.oz, t, bar);
+  }
+  if (!mbar_wait(bar, 0, kTmaWaitPolls)) tile_load<T>(tile, grid, st, g);
+}
+
+// Host: encode the tensor map of `ntr` fine grids at `grid` for tiles of a
+// (bs + ns - 1)^DIM box.  Returns false (the kernel then loads every tile
+// cell by cell) where a rule of tiled bulk copies would be broken: a start
+// address or row pitch off 16 bytes, an FP32 box row of an odd number of
+// cells (its byte width must be a multiple of 16), an odd FP32 bin width
+// (tile x origins must sit on 16 bytes), a box side above 256, or no
+// encoder in the driver.  CUFINUFFT_TMA=0 turns the bulk copies off.
+template <typename T, int DIM>
+bool grid_tensor_map(CUtensorMap* map, const cplx_t<T>* grid, const GridGeom& g, int ntr, const int bs[3],
+                     int ns) {
+  using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static const Encode encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return reinterpret_cast<Encode>(fn);
+  }();
+  if (const char* v = std::getenv("CUFINUFFT_TMA"))
+    if (v[0] == '0') return false;
+  if (!encode || grid == nullptr || ntr < 1) return false;
+  const int TX = bs[0] + ns - 1, TY = DIM > 1 ? bs[1] + ns - 1 : 1, TZ = DIM > 2 ? bs[2] + ns - 1 : 1;
+  constexpr size_t C = sizeof(cplx_t<T>);
+  if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0) return false;
+  if (sizeof(T) == 4 && ((TX & 1) || (bs[0] & 1))) return false;
+  if (2 * TX > 256 || TY > 256 || TZ > 256) return false;
+  if (TX > g.nf[0] || TY > g.nf[1] || TZ > g.nf[2]) return false;
+  cuuint64_t dims[4], strides[3];
+  cuuint32_t box[4], estr[4] = {1, 1, 1, 1};
+  int r = 0;
+  dims[r] = 2ull * g.nf[0];
+  box[r++] = 2u * TX;
+  size_t pitch = (size_t)g.nf[0] * C;
+  if (DIM > 1) { strides[r - 1] = pitch; dims[r] = g.nf[1]; box[r++] = TY; pitch *= g.nf[1]; }
+  if (DIM > 2) { strides[r - 1] = pitch; dims[r] = g.nf[2]; box[r++] = TZ; }
+  strides[r - 1] = (size_t)g.Nf * C;
+  dims[r] = ntr;
+  box[r++] = 1;
+  for (int i = 0; i < r - 1; ++i)
+    if (strides[i] % 16 != 0 || strides[i] >= (1ull << 40)) return false;
+  std::memset(map, 0, sizeof(*map));
+  const CUresult e = encode(map, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                            (cuuint32_t)r, const_cast<cplx_t<T>*>(grid), dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return e == CUDA_SUCCESS;
 }
 
 template <typename T>
@@ -286,16 +380,22 @@ k_interp_gm(SpreadArgs<T> a) {
 // Method 2: shared-memory subproblem interpolation.  grid = (nsub, ntr).
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads, sizeof(T) == 4 ? (NS <= 9 ? 6 : 4) : 1)  // FP32 ns <= 9: 40 regs, 6 blocks/SM
-k_interp_sm(SpreadArgs<T> a) {
+k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) {
   using C = cplx_t<T>;
   constexpr int HD = horner_degree<T>(NS);
   constexpr int NY = DIM > 1 ? NS : 1;
   constexpr int NZ = DIM > 2 ? NS : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  C* tile = reinterpret_cast<C*>(smem_raw);
+  __shared__ __align__(8) unsigned long long tile_bar;
+  C* tile = reinterpret_cast<C*>(tma ? smem_align128(smem_raw) : smem_raw);
+  if (tma && threadIdx.x == 0) mbar_init(&tile_bar, 1);  // visible after the sync in sub_tile_block
   const SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
   const int t = blockIdx.y;
-  tile_load<T>(tile, a.fw_in + (size_t)t * a.g.Nf, st, a.g);
+  const C* src = a.fw_in + (size_t)t * a.g.Nf;
+  if (tma && tile_inside<DIM>(st, a.g) && (sizeof(T) == 8 || (st.ox & 1) == 0))
+    tile_load_tma<T, DIM>(tile, &gmap, st, t, &tile_bar, src, a.g);
+  else
+    tile_load<T>(tile, src, st, a.g);
   __syncthreads();
   for (int p = st.p0 + threadIdx.x; p < st.p0 + st.np; p += blockDim.x) {
     T k1[NS], k2[NS];
@@ -891,12 +991,19 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
   } else {
     if (a.bins.nsub == 0) return cudaSuccess;
     size_t sm = tile_bytes<T, DIM>(NS, a.bins);
+    CUtensorMap gmap;
+    int tma = 0;
+    if (!wc) {
+      std::memset(&gmap, 0, sizeof(gmap));
+      tma = grid_tensor_map<T, DIM>(&gmap, a.fw_in, a.g, a.ntr, a.bins.bs, NS) ? 1 : 0;
+      if (tma) sm += 128;  // room to align the tile for the bulk copy
+    }
     cudaError_t e = wc ? prepare_smem(k_interp_sm_wc<T, DIM, NS>, sm)
                        : prepare_smem(k_interp_sm<T, DIM, NS>, sm);
     if (e != cudaSuccess) return e;
     dim3 grid(a.bins.nsub, a.ntr);
     if (wc) k_interp_sm_wc<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
-    else k_interp_sm<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
+    else k_interp_sm<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a, gmap, tma);
   }
   return cudaGetLastError();
 }
