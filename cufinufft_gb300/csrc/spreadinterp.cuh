@@ -90,13 +90,19 @@ struct TileRows {
   }
 };
 
+// True when the tile lies inside the grid (no periodic wrap on any axis;
+// the unused axes have nf = 1, origin 0 and extent 1).
+__device__ __forceinline__ bool tile_in_grid(const SubTile& st, const GridGeom& g) {
+  return st.ox + st.TX <= g.nf[0] && st.oy + st.TY <= g.nf[1] && st.oz + st.TZ <= g.nf[2];
+}
+
 // Copy the subproblem's padded tile from the fine grid (periodic wrap) into
 // shared memory: one warp per tile row, lanes along x.  Tile coordinates
 // stay below 3 nf (bins within the grid, halo ns - 1 <= nf / 2), so two
 // conditional subtractions wrap them.
 template <typename T>
-__device__ __forceinline__ void tile_load(cplx_t<T>* tile, const cplx_t<T>* grid, const SubTile& st,
-                                          const GridGeom& g) {
+__device__ __forceinline__ void tile_load_periodic(cplx_t<T>* tile, const cplx_t<T>* grid, const SubTile& st,
+                                                   const GridGeom& g) {
   const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
   const int rows = st.TY * st.TZ;
   TileRows rw(threadIdx.x >> 5, st.TY);
@@ -114,6 +120,28 @@ __device__ __forceinline__ void tile_load(cplx_t<T>* tile, const cplx_t<T>* grid
   cp_async_wait();  // this thread's copies have landed; the caller syncs the block
 }
 
+// Same, without the per-cell wrap where the tile lies inside the grid.
+template <typename T>
+__device__ __forceinline__ void tile_load(cplx_t<T>* tile, const cplx_t<T>* grid, const SubTile& st,
+                                          const GridGeom& g) {
+  if (!tile_in_grid(st, g)) {
+    tile_load_periodic<T>(tile, grid, st, g);
+    return;
+  }
+  const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
+  const int rows = st.TY * st.TZ;
+  TileRows rw(threadIdx.x >> 5, st.TY);
+  for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
+    const cplx_t<T>* src = grid + ((size_t)(st.oz + rw.iz) * g.nf[1] + st.oy + rw.iy) * g.nf[0] + st.ox;
+    cplx_t<T>* dst = tile + r * st.TX;
+    for (int ix = lane; ix < st.TX; ix += 32) {
+      if constexpr (sizeof(T) == 4) cp_async8(dst + ix, src + ix);
+      else cp_async16(dst + ix, src + ix);
+    }
+  }
+  cp_async_wait();
+}
+
 // Add the tile back into the fine grid with vector reductions, skipping the
 // cells no point touched.
 template <typename T>
@@ -122,6 +150,18 @@ __device__ __forceinline__ void tile_flush(const cplx_t<T>* tile, cplx_t<T>* gri
   const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
   const int rows = st.TY * st.TZ;
   TileRows rw(threadIdx.x >> 5, st.TY);
+  if (tile_in_grid(st, g)) {  // no wrap
+    for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
+      cplx_t<T>* dst = grid + ((size_t)(st.oz + rw.iz) * g.nf[1] + st.oy + rw.iy) * g.nf[0] + st.ox;
+      const cplx_t<T>* src = tile + r * st.TX;
+      for (int ix = lane; ix < st.TX; ix += 32) {
+        const cplx_t<T> v = src[ix];
+        if (v.x == T(0) && v.y == T(0)) continue;
+        red_add(dst + ix, v.x, v.y);
+      }
+    }
+    return;
+  }
   for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
     const int gy = wrap3(st.oy + rw.iy, g.nf[1]), gz = wrap3(st.oz + rw.iz, g.nf[2]);
     cplx_t<T>* dst = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
@@ -146,10 +186,12 @@ __device__ __forceinline__ void tile_flush(const cplx_t<T>* tile, cplx_t<T>* gri
 // loads its share of the tile itself (the data is the same either way).
 constexpr int kTmaWaitPolls = 1 << 20;
 
-template <int DIM>
-__device__ __forceinline__ bool tile_inside(const SubTile& st, const GridGeom& g) {
-  return st.ox + st.TX <= g.nf[0] && (DIM < 2 || st.oy + st.TY <= g.nf[1]) &&
-         (DIM < 3 || st.oz + st.TZ <= g.nf[2]);
+// Tile row length (cells) of a bulk-copied tile: a box row must be a
+// multiple of 16 bytes, so FP32 rows of an odd number of cells take one
+// more cell (its value is loaded and never used).
+template <typename T>
+__host__ __device__ __forceinline__ int bulk_tile_x(int TX) {
+  return sizeof(T) == 4 ? (TX + 1) & ~1 : TX;
 }
 
 // Shared-memory start of the tile rounded up to 128 bytes (bulk tensor
@@ -158,26 +200,32 @@ __device__ __forceinline__ unsigned char* smem_align128(unsigned char* p) {
   return p + ((128u - (smem_u32(p) & 127u)) & 127u);
 }
 
+// Thread 0: start the tile's bulk copy.
 template <typename T, int DIM>
-__device__ __forceinline__ void tile_load_tma(cplx_t<T>* tile, const CUtensorMap* map, const SubTile& st,
-                                              int t, unsigned long long* bar, const cplx_t<T>* grid,
-                                              const GridGeom& g) {
-  if (threadIdx.x == 0) {
-    mbar_expect_tx(bar, (unsigned)(st.ntile * sizeof(cplx_t<T>)));
-    if constexpr (DIM == 1) tma_load2(tile, map, 2 * st.ox, t, bar);
-    else if constexpr (DIM == 2) tma_load3(tile, map, 2 * st.ox, st.oy, t, bar);
-    else tma_load4(tile, map, 2 * st.ox, st.oy, st.oz, t, bar);
-  }
-  if (!mbar_wait(bar, 0, kTmaWaitPolls)) tile_load<T>(tile, grid, st, g);
+__device__ __forceinline__ void tile_copy_start(cplx_t<T>* tile, const CUtensorMap* map, const SubTile& st,
+                                                int t, unsigned long long* bar) {
+  mbar_expect_tx(bar, (unsigned)(st.ntile * sizeof(cplx_t<T>)));
+  if constexpr (DIM == 1) tma_load2(tile, map, 2 * st.ox, t, bar);
+  else if constexpr (DIM == 2) tma_load3(tile, map, 2 * st.ox, st.oy, t, bar);
+  else tma_load4(tile, map, 2 * st.ox, st.oy, st.oz, t, bar);
+}
+
+// Every thread: wait for the bulk copy; a thread whose wait runs out loads
+// its share of the tile cell by cell instead (the same values; the caller
+// syncs the block afterwards).
+template <typename T>
+__device__ __forceinline__ void tile_copy_wait(cplx_t<T>* tile, unsigned long long* bar, const cplx_t<T>* grid,
+                                               const SubTile& st, const GridGeom& g) {
+  if (!mbar_wait(bar, 0, kTmaWaitPolls)) tile_load_periodic<T>(tile, grid, st, g);
 }
 
 // Host: encode the tensor map of `ntr` fine grids at `grid` for tiles of a
-// (bs + ns - 1)^DIM box.  Returns false (the kernel then loads every tile
-// cell by cell) where a rule of tiled bulk copies would be broken: a start
-// address or row pitch off 16 bytes, an FP32 box row of an odd number of
-// cells (its byte width must be a multiple of 16), an odd FP32 bin width
-// (tile x origins must sit on 16 bytes), a box side above 256, or no
-// encoder in the driver.  CUFINUFFT_TMA=0 turns the bulk copies off.
+// bulk_tile_x(bs0 + ns - 1) x (bs1 + ns - 1) x (bs2 + ns - 1) box.  Returns
+// false (the kernel then loads every tile cell by cell) where a rule of
+// tiled bulk copies would be broken: a start address or row pitch off 16
+// bytes, an odd FP32 bin width (tile x origins must sit on 16 bytes), a box
+// side above 256, or no encoder in the driver.  CUFINUFFT_TMA=0 turns the
+// bulk copies off.
 template <typename T, int DIM>
 bool grid_tensor_map(CUtensorMap* map, const cplx_t<T>* grid, const GridGeom& g, int ntr, const int bs[3],
                      int ns) {
@@ -196,10 +244,11 @@ bool grid_tensor_map(CUtensorMap* map, const cplx_t<T>* grid, const GridGeom& g,
   if (const char* v = std::getenv("CUFINUFFT_TMA"))
     if (v[0] == '0') return false;
   if (!encode || grid == nullptr || ntr < 1) return false;
-  const int TX = bs[0] + ns - 1, TY = DIM > 1 ? bs[1] + ns - 1 : 1, TZ = DIM > 2 ? bs[2] + ns - 1 : 1;
+  const int TX = bulk_tile_x<T>(bs[0] + ns - 1), TY = DIM > 1 ? bs[1] + ns - 1 : 1,
+            TZ = DIM > 2 ? bs[2] + ns - 1 : 1;
   constexpr size_t C = sizeof(cplx_t<T>);
   if ((reinterpret_cast<uintptr_t>(grid) & 15) != 0) return false;
-  if (sizeof(T) == 4 && ((TX & 1) || (bs[0] & 1))) return false;
+  if (sizeof(T) == 4 && (bs[0] & 1)) return false;
   if (2 * TX > 256 || TY > 256 || TZ > 256) return false;
   if (TX > g.nf[0] || TY > g.nf[1] || TZ > g.nf[2]) return false;
   cuuint64_t dims[4], strides[3];
@@ -378,33 +427,35 @@ k_interp_gm(SpreadArgs<T> a) {
 
 // ---------------------------------------------------------------------------
 // Method 2: shared-memory subproblem interpolation.  grid = (nsub, ntr).
+
+// One point's tile offsets and kernel rows: everything the taps need except
+// the tile itself.
 template <typename T, int DIM, int NS>
-__global__ void __launch_bounds__(kSpreadThreads, sizeof(T) == 4 ? (NS <= 9 ? 6 : 4) : 1)  // FP32 ns <= 9: 40 regs, 6 blocks/SM
-k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) {
-  using C = cplx_t<T>;
-  constexpr int HD = horner_degree<T>(NS);
-  constexpr int NY = DIM > 1 ? NS : 1;
-  constexpr int NZ = DIM > 2 ? NS : 1;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ __align__(8) unsigned long long tile_bar;
-  C* tile = reinterpret_cast<C*>(tma ? smem_align128(smem_raw) : smem_raw);
-  if (tma && threadIdx.x == 0) mbar_init(&tile_bar, 1);  // visible after the sync in sub_tile_block
-  const SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
-  const int t = blockIdx.y;
-  const C* src = a.fw_in + (size_t)t * a.g.Nf;
-  if (tma && tile_inside<DIM>(st, a.g) && (sizeof(T) == 8 || (st.ox & 1) == 0))
-    tile_load_tma<T, DIM>(tile, &gmap, st, t, &tile_bar, src, a.g);
-  else
-    tile_load<T>(tile, src, st, a.g);
-  __syncthreads();
-  for (int p = st.p0 + threadIdx.x; p < st.p0 + st.np; p += blockDim.x) {
-    T k1[NS], k2[NS];
-    const int lx = a.pts.i0[0][p] - st.ox;
-    kernel_row<T, NS, HD>(a.pts.d[0][p], a.kc, k1);
-    int ly = 0, lz = 0;
-    if (DIM > 1) { ly = a.pts.i0[1][p] - st.oy; kernel_row<T, NS, HD>(a.pts.d[1][p], a.kc, k2); }
-    T d3 = T(0);
+struct InterpPoint {
+  T k1[NS], k2[NS];
+  T d1, d2, d3;
+  int lx, ly, lz;
+  // the point's sorted coordinates (first tap, offset)
+  __device__ __forceinline__ void fetch(const SpreadArgs<T>& a, int p, const SubTile& st) {
+    lx = a.pts.i0[0][p] - st.ox;
+    d1 = a.pts.d[0][p];
+    ly = lz = 0;
+    d2 = d3 = T(0);
+    if (DIM > 1) { ly = a.pts.i0[1][p] - st.oy; d2 = a.pts.d[1][p]; }
     if (DIM > 2) { lz = a.pts.i0[2][p] - st.oz; d3 = a.pts.d[2][p]; }
+  }
+  // kernel rows along x and y (z values are evaluated per plane)
+  __device__ __forceinline__ void rows(const SpreadArgs<T>& a) {
+    constexpr int HD = horner_degree<T>(NS);
+    kernel_row<T, NS, HD>(d1, a.kc, k1);
+    if (DIM > 1) kernel_row<T, NS, HD>(d2, a.kc, k2);
+  }
+  __device__ __forceinline__ cplx_t<T> taps(const SpreadArgs<T>& a, const cplx_t<T>* tile,
+                                            const SubTile& st) const {
+    using C = cplx_t<T>;
+    constexpr int HD = horner_degree<T>(NS);
+    constexpr int NY = DIM > 1 ? NS : 1;
+    constexpr int NZ = DIM > 2 ? NS : 1;
     C out;
     if constexpr (sizeof(T) == 4) {
       // packed pairs: one fma.rn.f32x2 per complex tap (same IEEE fmas)
@@ -455,7 +506,46 @@ k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) 
       out.x = ar;
       out.y = ai;
     }
-    a.c_out[(size_t)t * a.M + a.pts.idx[p]] = out;
+    return out;
+  }
+};
+
+// The coordinates of every thread's first point are read while the tile is
+// still on its way (the bulk copy runs in the background; the per-cell path
+// is asynchronous up to its wait).  Its kernel rows are evaluated after the
+// wait: evaluated before it, the rows stay live across the wait and the FP32
+// kernels spill at the 40-register bound (measured 3.5% slower).
+template <typename T, int DIM, int NS>
+__global__ void __launch_bounds__(kSpreadThreads, sizeof(T) == 4 ? (NS <= 9 ? 6 : 4) : 1)  // FP32 ns <= 9: 40 regs, 6 blocks/SM
+k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) {
+  using C = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long tile_bar;
+  C* tile = reinterpret_cast<C*>(tma ? smem_align128(smem_raw) : smem_raw);
+  if (tma && threadIdx.x == 0) mbar_init(&tile_bar, 1);  // visible after the sync in sub_tile_block
+  SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
+  if (tma) {  // the tile row widened as the tensor map's box is (bulk_tile_x)
+    st.TX = bulk_tile_x<T>(st.TX);
+    st.ntile = st.TX * st.TY * st.TZ;
+  }
+  const int t = blockIdx.y;
+  const C* src = a.fw_in + (size_t)t * a.g.Nf;
+  const bool bulk = tma && tile_in_grid(st, a.g) && (sizeof(T) == 8 || (st.ox & 1) == 0);
+  if (bulk && threadIdx.x == 0) tile_copy_start<T, DIM>(tile, &gmap, st, t, &tile_bar);
+  const int p_end = st.p0 + st.np;
+  int p = st.p0 + threadIdx.x;
+  InterpPoint<T, DIM, NS> pt;
+  if (!bulk) tile_load_periodic<T>(tile, src, st, a.g);
+  if (p < p_end) pt.fetch(a, p, st);
+  if (bulk) tile_copy_wait<T>(tile, &tile_bar, src, st, a.g);
+  __syncthreads();
+  if (p >= p_end) return;
+  pt.rows(a);
+  a.c_out[(size_t)t * a.M + a.pts.idx[p]] = pt.taps(a, tile, st);
+  for (p += blockDim.x; p < p_end; p += blockDim.x) {
+    pt.fetch(a, p, st);
+    pt.rows(a);
+    a.c_out[(size_t)t * a.M + a.pts.idx[p]] = pt.taps(a, tile, st);
   }
 }
 
@@ -592,6 +682,19 @@ __device__ __forceinline__ void plane_flush(const T* re, const T* im, cplx_t<T>*
   const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
   const int rows = st.TY * st.TZ;
   TileRows rw(threadIdx.x >> 5, st.TY);
+  if (tile_in_grid(st, g)) {  // no wrap
+    for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
+      cplx_t<T>* dst = grid + ((size_t)(st.oz + rw.iz) * g.nf[1] + st.oy + rw.iy) * g.nf[0] + st.ox;
+      const T* rr = re + r * st.TX;
+      const T* ri = im + r * st.TX;
+      for (int ix = lane; ix < st.TX; ix += 32) {
+        const T vr = rr[ix], vi = ri[ix];
+        if (vr == T(0) && vi == T(0)) continue;
+        red_add(dst + ix, vr, vi);
+      }
+    }
+    return;
+  }
   for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
     const int gy = wrap3(st.oy + rw.iy, g.nf[1]), gz = wrap3(st.oz + rw.iz, g.nf[2]);
     cplx_t<T>* dst = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
@@ -996,7 +1099,17 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
     if (!wc) {
       std::memset(&gmap, 0, sizeof(gmap));
       tma = grid_tensor_map<T, DIM>(&gmap, a.fw_in, a.g, a.ntr, a.bins.bs, NS) ? 1 : 0;
-      if (tma) sm += 128;  // room to align the tile for the bulk copy
+      if (tma) {
+        // widened rows, and room to align the tile for the bulk copy
+        const int tx = a.bins.bs[0] + NS - 1;
+        const size_t smb = sm / tx * bulk_tile_x<T>(tx) + 128;
+        int dev = 0, optin = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e != cudaSuccess) return e;
+        if (smb <= (size_t)optin) sm = smb;
+        else tma = 0;
+      }
     }
     cudaError_t e = wc ? prepare_smem(k_interp_sm_wc<T, DIM, NS>, sm)
                        : prepare_smem(k_interp_sm<T, DIM, NS>, sm);

@@ -17,7 +17,7 @@ CASES = [
     # (modes, single, tol, bins)
     ((100, 120), True, 1e-6, None),              # 2D default bins, TX 38
     ((100, 120), False, 1e-9, None),             # 2D FP64, TX 41 (odd is fine for 16-byte cells)
-    ((64, 70), True, 1e-5, None),                # ns 6: odd FP32 box row, per-cell path
+    ((64, 70), True, 1e-5, None),                # ns 6: odd FP32 tile row, widened by one cell
     ((64, 70), True, 1e-6, (31, 16, 1)),         # odd FP32 bin width, per-cell path
     ((24, 30, 20), True, 1e-6, None),            # 3D
     ((24, 30, 20), False, 1e-8, None),           # 3D FP64
