@@ -115,6 +115,8 @@ template <typename T> static void release(Plan<T>* p) {
   cudaFree(p->sub_start);
   cudaFree(p->scan_tmp);
   cudaFree(p->sub_to_bin);
+  cudaFree(p->sub_hdr);
+  p->sub_hdr = nullptr;
   p->count = p->start = p->sub_start = p->scan_tmp = p->sub_to_bin = nullptr;
   p->cap_sub = 0;
   cudaFree(p->cls_count);
@@ -879,12 +881,16 @@ static int build_subproblems(Plan<T>* p) {
   const int nsub = *p->h_total;
   if ((size_t)nsub > p->cap_sub) {
     cudaFree(p->sub_to_bin);
+    cudaFree(p->sub_hdr);
     p->sub_to_bin = nullptr;
+    p->sub_hdr = nullptr;
     p->cap_sub = 0;
     CFG_CUDA(cudaMalloc(&p->sub_to_bin, sizeof(int) * (size_t)nsub));
+    CFG_CUDA(cudaMalloc(&p->sub_hdr, sizeof(SubHdr) * (size_t)nsub));
     p->cap_sub = nsub;
   }
-  CFG_CUDA(launch_sub_to_bin(p->sub_start, p->nbins, nsub, p->sub_to_bin, p->stream));
+  CFG_CUDA(launch_sub_headers(p->sub_start, p->start, p->count, p->nbins, nsub, ms, p->bs, p->nb,
+                              p->sub_to_bin, p->sub_hdr, p->stream));
   p->nsub = nsub;
   if (p->cell_order) {
     if ((size_t)nsub > p->cap_sub_dense) {

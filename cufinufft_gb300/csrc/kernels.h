@@ -109,6 +109,11 @@ struct SubClassArgs {
 cudaError_t launch_classify_subproblems(const SubClassArgs& a, cudaStream_t s);
 cudaError_t launch_sub_to_bin(const int* sub_start, int nbins, int nsub, int* sub_to_bin,
                               cudaStream_t s);
+// sub_to_bin plus the subproblem headers (hdr[nsub]) of bins bs x nb holding
+// count[b] points from start[b] on, at most maxsub per subproblem.
+cudaError_t launch_sub_headers(const int* sub_start, const int* start, const int* count, int nbins,
+                               int nsub, int maxsub, const int bs[3], const int nb[3], int* sub_to_bin,
+                               SubHdr* hdr, cudaStream_t s);
 
 // deconv.cu
 struct FseriesNodes {

@@ -60,6 +60,13 @@ struct GridGeom {
   long long Nf;       // nf1*nf2*nf3
 };
 
+// Per-subproblem header written at setpts: first sorted point, point
+// count, tile origin (cells).  Two 16-byte words.
+struct __align__(16) SubHdr {
+  int p0, np, ox, oy;
+  int oz, pad0, pad1, pad2;
+};
+
 struct BinTables {
   int bs[3];          // bin size (cells) per axis
   int nb[3];          // bins per axis
@@ -70,6 +77,7 @@ struct BinTables {
   const int* sub_to_bin;  // subproblem -> bin          [nsub]
   int nsub;
   int maxsub;             // points per subproblem cap
+  const SubHdr* hdr;      // subproblem headers [nsub], or null (derived from the tables above)
 };
 
 // Everything a spread or interp launch needs.

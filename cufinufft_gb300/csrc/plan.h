@@ -59,6 +59,7 @@ template <typename T> struct Plan {
   int* sub_start = nullptr;
   int* scan_tmp = nullptr;
   int* sub_to_bin = nullptr;
+  SubHdr* sub_hdr = nullptr;  // [cap_sub] subproblem headers
   size_t cap_sub = 0;
   int* cls_count = nullptr;  // per (bin, class) counts for method 2 ordering
   size_t cap_cls = 0;
@@ -166,6 +167,7 @@ inline SpreadArgs<T> spread_args(Plan<T>* p) {
   a.bins.start = p->start;
   a.bins.sub_start = p->sub_start;
   a.bins.sub_to_bin = p->sub_to_bin;
+  a.bins.hdr = p->sub_hdr;
   a.bins.nsub = p->nsub;
   a.bins.maxsub = p->opts.gpu_maxsubprobsize;
   a.kc.beta = (T)p->sp.beta;

@@ -462,4 +462,58 @@ cudaError_t launch_sub_to_bin(const int* sub_start, int nbins, int nsub, int* su
   return cudaGetLastError();
 }
 
+struct SubHdrArgs {
+  const int *sub_start, *start, *count;
+  int nbins, nsub, maxsub;
+  int bs[3], nb[3];
+  int* sub_to_bin;
+  SubHdr* hdr;
+};
+
+// The same bin search as k_sub_to_bin, then the subproblem's point range
+// (subproblem js of bin b: points start[b] + js maxsub, at most maxsub of
+// them) and its tile origin (the bin's first cell).
+__global__ void k_sub_headers(SubHdrArgs a) {
+  for (int sidx = blockIdx.x * blockDim.x + threadIdx.x; sidx < a.nsub; sidx += gridDim.x * blockDim.x) {
+    int lo = 0, hi = a.nbins;
+    while (hi - lo > 1) {
+      int mid = (lo + hi) >> 1;
+      if (a.sub_start[mid] <= sidx) lo = mid;
+      else hi = mid;
+    }
+    const int b = lo;
+    a.sub_to_bin[sidx] = b;
+    const int js = sidx - a.sub_start[b];
+    SubHdr h;
+    h.p0 = a.start[b] + js * a.maxsub;
+    h.np = min(a.maxsub, a.count[b] - js * a.maxsub);
+    h.ox = (b % a.nb[0]) * a.bs[0];
+    h.oy = ((b / a.nb[0]) % a.nb[1]) * a.bs[1];
+    h.oz = (b / (a.nb[0] * a.nb[1])) * a.bs[2];
+    h.pad0 = h.pad1 = h.pad2 = 0;
+    a.hdr[sidx] = h;
+  }
+}
+
+cudaError_t launch_sub_headers(const int* sub_start, const int* start, const int* count, int nbins,
+                               int nsub, int maxsub, const int bs[3], const int nb[3], int* sub_to_bin,
+                               SubHdr* hdr, cudaStream_t s) {
+  if (nsub <= 0) return cudaSuccess;
+  SubHdrArgs a;
+  a.sub_start = sub_start;
+  a.start = start;
+  a.count = count;
+  a.nbins = nbins;
+  a.nsub = nsub;
+  a.maxsub = maxsub;
+  for (int k = 0; k < 3; ++k) {
+    a.bs[k] = bs[k];
+    a.nb[k] = nb[k];
+  }
+  a.sub_to_bin = sub_to_bin;
+  a.hdr = hdr;
+  k_sub_headers<<<place_grid(nsub), kPlaceThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
 }  // namespace cfg

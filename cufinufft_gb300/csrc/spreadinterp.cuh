@@ -57,6 +57,24 @@ __device__ __forceinline__ SubTile sub_tile(const BinTables& bt, int sub) {
   return s;
 }
 
+// sub_tile from the subproblem's precomputed header: every thread reads the
+// same 16 (3D: 32) bytes, no block barrier.
+template <int DIM, int NS>
+__device__ __forceinline__ SubTile sub_tile_hdr(const BinTables& bt, int sub) {
+  const int4 h = __ldg(reinterpret_cast<const int4*>(bt.hdr + sub));
+  SubTile s;
+  s.p0 = h.x;
+  s.np = h.y;
+  s.ox = h.z;
+  s.oy = h.w;
+  s.oz = DIM > 2 ? __ldg(&bt.hdr[sub].oz) : 0;
+  s.TX = bt.bs[0] + NS - 1;
+  s.TY = DIM > 1 ? bt.bs[1] + NS - 1 : 1;
+  s.TZ = DIM > 2 ? bt.bs[2] + NS - 1 : 1;
+  s.ntile = s.TX * s.TY * s.TZ;
+  return s;
+}
+
 // sub_tile computed once per block (three integer divisions) and shared
 // through shared memory; PERSISTENT blocks (several subproblems each) first
 // wait until every thread is done with the previous one.
@@ -522,8 +540,9 @@ k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) unsigned long long tile_bar;
   C* tile = reinterpret_cast<C*>(tma ? smem_align128(smem_raw) : smem_raw);
-  if (tma && threadIdx.x == 0) mbar_init(&tile_bar, 1);  // visible after the sync in sub_tile_block
-  SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
+  if (tma && threadIdx.x == 0) mbar_init(&tile_bar, 1);
+  SubTile st = sub_tile_hdr<DIM, NS>(a.bins, blockIdx.x);  // loads in flight across the barrier
+  if (tma) __syncthreads();                                 // the barrier's init before any wait on it
   if (tma) {  // the tile row widened as the tensor map's box is (bulk_tile_x)
     st.TX = bulk_tile_x<T>(st.TX);
     st.ntile = st.TX * st.TY * st.TZ;
@@ -1093,6 +1112,7 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
     }
   } else {
     if (a.bins.nsub == 0) return cudaSuccess;
+    if (!wc && a.bins.hdr == nullptr) return cudaErrorInvalidValue;  // k_interp_sm reads the headers
     size_t sm = tile_bytes<T, DIM>(NS, a.bins);
     CUtensorMap gmap;
     int tma = 0;
