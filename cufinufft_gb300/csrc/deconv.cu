@@ -62,6 +62,9 @@ cudaError_t launch_fseries(const FseriesNodes& nodes, int dim, const int nf[3], 
 }
 
 // One block row per (k2, k3) mode row; threads over k1.
+// Cells per thread per pass of the row kernels below.
+constexpr int kRowUnroll = 4;
+
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_deconvolve(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, const cplx_t<T>* __restrict__ fw,
@@ -83,15 +86,31 @@ k_deconvolve(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, const c
     if (dim > 2) f23 *= fac2[i3];
     const C* src = fw + (size_t)t * Nf + ((size_t)w3 * nf1 + w2) * nf0;
     C* dst = fk + (size_t)t * Nm + ((size_t)i3 * N1 + i2) * N0;
-    for (int i1 = threadIdx.x; i1 < N0; i1 += blockDim.x) {
-      const int k1 = i1 - N0 / 2;
-      const int w1 = k1 >= 0 ? k1 : nf0 + k1;
-      const T f = fac0[i1] * f23;
-      const C v = src[w1];
-      C o;
-      o.x = v.x * f;
-      o.y = v.y * f;
-      dst[i1] = o;
+    // kRowUnroll cells per thread with every load issued before the first
+    // store: a row's reads are in flight together
+    for (int b = threadIdx.x; b < N0; b += kRowUnroll * blockDim.x) {
+      C v[kRowUnroll];
+      T f[kRowUnroll];
+#pragma unroll
+      for (int u = 0; u < kRowUnroll; ++u) {
+        const int i1 = b + u * blockDim.x;
+        if (i1 < N0) {
+          const int k1 = i1 - N0 / 2;
+          v[u] = src[k1 >= 0 ? k1 : nf0 + k1];
+          f[u] = fac0[i1];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kRowUnroll; ++u) {
+        const int i1 = b + u * blockDim.x;
+        if (i1 < N0) {
+          const T g = f[u] * f23;
+          C o;
+          o.x = v[u].x * g;
+          o.y = v[u].y * g;
+          dst[i1] = o;
+        }
+      }
     }
   }
 }
@@ -135,15 +154,29 @@ k_amplify_modes(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, cplx
     if (dim > 2) f23 *= fac2[i3];
     C* dst = fw + (size_t)t * Nf + ((size_t)w3 * nf1 + w2) * nf0;
     const C* src = fk + (size_t)t * Nm + ((size_t)i3 * N1 + i2) * N0;
-    for (int i1 = threadIdx.x; i1 < N0; i1 += blockDim.x) {
-      const int k1 = i1 - N0 / 2;
-      const int w1 = k1 >= 0 ? k1 : nf0 + k1;
-      const T f = fac0[i1] * f23;
-      const C v = src[i1];
-      C o;
-      o.x = v.x * f;
-      o.y = v.y * f;
-      dst[w1] = o;
+    for (int b = threadIdx.x; b < N0; b += kRowUnroll * blockDim.x) {
+      C v[kRowUnroll];
+      T f[kRowUnroll];
+#pragma unroll
+      for (int u = 0; u < kRowUnroll; ++u) {
+        const int i1 = b + u * blockDim.x;
+        if (i1 < N0) {
+          v[u] = src[i1];
+          f[u] = fac0[i1];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kRowUnroll; ++u) {
+        const int i1 = b + u * blockDim.x;
+        if (i1 < N0) {
+          const int k1 = i1 - N0 / 2;
+          const T g = f[u] * f23;
+          C o;
+          o.x = v[u].x * g;
+          o.y = v[u].y * g;
+          dst[k1 >= 0 ? k1 : nf0 + k1] = o;
+        }
+      }
     }
   }
 }

@@ -116,6 +116,31 @@ __device__ __forceinline__ T es_eval(T z, const KernelCoeffs<T>& kc) {
 // kc.horner set the values come from the plan's fitted piecewise
 // polynomials in z = 2d - 1 (coefficient k of tap j at coef[k*NS + j],
 // highest degree first, HDEG+1 rows).
+// FP32 row of ES values two taps at a time: es_value_fast's steps on each
+// tap, the plain multiplies and adds as packed f32x2 instructions (each half
+// an IEEE operation; 1 - z is rounded after z, where the compiler may fuse
+// the scalar form into one fma, so values can differ from it by an ulp).
+template <int NS>
+__device__ __forceinline__ void es_row_f32x2(float d, const KernelCoeffs<float>& kc, float* ker) {
+  const float x0 = d - 0.5f * NS;
+  const float2 c2 = make_float2(kc.c, kc.c), one = make_float2(1.0f, 1.0f);
+  const float2 mone = make_float2(-1.0f, -1.0f), mb = make_float2(-kc.bl2e, -kc.bl2e);
+  const float2 eb = make_float2(kc.e_beta, kc.e_beta);
+#pragma unroll
+  for (int j = 0; j + 1 < NS; j += 2) {
+    const float2 x = __fadd2_rn(make_float2(x0, x0), make_float2(float(j), float(j + 1)));
+    const float2 z = __fmul2_rn(__fmul2_rn(c2, x), x);
+    const float2 u = __ffma2_rn(z, mone, one);  // 1 - z
+    const float2 s = make_float2(sqrt_approx(fmaxf(u.x, 0.0f)), sqrt_approx(fmaxf(u.y, 0.0f)));
+    const float2 q = __fadd2_rn(one, s);
+    const float2 e = __fmul2_rn(__fmul2_rn(mb, z), make_float2(rcp_approx(q.x), rcp_approx(q.y)));
+    const float2 v = __fmul2_rn(make_float2(ex2_approx(e.x), ex2_approx(e.y)), eb);
+    ker[j] = z.x < 1.0f ? v.x : 0.0f;
+    ker[j + 1] = z.y < 1.0f ? v.y : 0.0f;
+  }
+  if (NS & 1) ker[NS - 1] = es_value_fast(kc.c * (x0 + float(NS - 1)) * (x0 + float(NS - 1)), kc.e_beta, kc.bl2e);
+}
+
 template <typename T, int NS, int HDEG>
 __device__ __forceinline__ void kernel_row(T d, const KernelCoeffs<T>& kc, T* ker) {
   if (kc.horner) {
@@ -127,6 +152,8 @@ __device__ __forceinline__ void kernel_row(T d, const KernelCoeffs<T>& kc, T* ke
 #pragma unroll
       for (int j = 0; j < NS; ++j) ker[j] = fma_rn(ker[j], z, kc.coef[k * NS + j]);
     }
+  } else if constexpr (sizeof(T) == 4) {
+    es_row_f32x2<NS>(d, kc, ker);
   } else {
     const T x0 = d - T(0.5) * T(NS);
 #pragma unroll
