@@ -61,136 +61,132 @@ cudaError_t launch_fseries(const FseriesNodes& nodes, int dim, const int nf[3], 
   return cudaGetLastError();
 }
 
-// One block row per (k2, k3) mode row; threads over k1.
-// Cells per thread per pass of the row kernels below.
+// Deconvolution and amplification move data between the mode cube and the
+// mode cells of the fine grid, one mode row (fixed k2, k3) at a time.  A
+// block is tx x ty threads: ty rows, tx threads along a row, each thread
+// kRowUnroll cells of its row per pass with every load issued before the
+// first store; long rows are split into chunks of kRowUnroll tx cells
+// (blockIdx.x = row block * nchunks + chunk), blockIdx.y = transform.
 constexpr int kRowUnroll = 4;
 
-template <typename T>
+template <typename T> struct ModeRows {
+  int nf0, nf1, nf2, N0, N1, N2;
+  int nrows, nchunks;
+  long long Nf, Nm;
+  const T *fac0, *fac1, *fac2;
+};
+
+// AMPLIFY false: fk[mode] = fw[cell] * fac (type 1); true: fw[cell] =
+// fk[mode] * fac (type 2).
+template <typename T, int DIM, bool AMPLIFY>
 __global__ void __launch_bounds__(256)
-k_deconvolve(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, const cplx_t<T>* __restrict__ fw,
-             cplx_t<T>* __restrict__ fk, const T* __restrict__ fac0, const T* __restrict__ fac1,
-             const T* __restrict__ fac2, int ntr) {
+k_mode_rows(ModeRows<T> m, const cplx_t<T>* __restrict__ in, cplx_t<T>* __restrict__ out) {
   using C = cplx_t<T>;
-  const long long Nf = (long long)nf0 * nf1 * nf2;
-  const long long Nm = (long long)N0 * N1 * N2;
-  const int nrows = N1 * N2;
-  for (int r = blockIdx.x; r < nrows * ntr; r += gridDim.x) {
-    const int t = r / nrows;
-    const int rr = r - t * nrows;
-    const int i2 = rr % N1, i3 = rr / N1;
-    const int k2 = i2 - N1 / 2, k3 = i3 - N2 / 2;
-    const int w2 = k2 >= 0 ? k2 : nf1 + k2;
-    const int w3 = k3 >= 0 ? k3 : nf2 + k3;
-    T f23 = T(1);
-    if (dim > 1) f23 = fac1[i2];
-    if (dim > 2) f23 *= fac2[i3];
-    const C* src = fw + (size_t)t * Nf + ((size_t)w3 * nf1 + w2) * nf0;
-    C* dst = fk + (size_t)t * Nm + ((size_t)i3 * N1 + i2) * N0;
-    // kRowUnroll cells per thread with every load issued before the first
-    // store: a row's reads are in flight together
-    for (int b = threadIdx.x; b < N0; b += kRowUnroll * blockDim.x) {
-      C v[kRowUnroll];
-      T f[kRowUnroll];
+  const unsigned rb = blockIdx.x / (unsigned)m.nchunks;
+  const int chunk = (int)(blockIdx.x - rb * (unsigned)m.nchunks);
+  const int rr = (int)rb * blockDim.y + threadIdx.y;
+  if (rr >= m.nrows) return;
+  const int t = blockIdx.y;
+  int i2 = 0, i3 = 0;
+  if (DIM == 2) i2 = rr;
+  if (DIM == 3) {
+    i3 = rr / m.N1;
+    i2 = rr - i3 * m.N1;
+  }
+  const int k2 = i2 - m.N1 / 2, k3 = i3 - m.N2 / 2;
+  const int w2 = k2 >= 0 ? k2 : m.nf1 + k2;
+  const int w3 = k3 >= 0 ? k3 : m.nf2 + k3;
+  T f23 = T(1);
+  if (DIM > 1) f23 = m.fac1[i2];
+  if (DIM > 2) f23 *= m.fac2[i3];
+  const size_t cell_row = (size_t)t * m.Nf + ((size_t)w3 * m.nf1 + w2) * m.nf0;
+  const size_t mode_row = (size_t)t * m.Nm + ((size_t)i3 * m.N1 + i2) * m.N0;
+  const C* src = in + (AMPLIFY ? mode_row : cell_row);
+  C* dst = out + (AMPLIFY ? cell_row : mode_row);
+  const int h0 = m.N0 / 2;
+  const int b = chunk * kRowUnroll * blockDim.x + threadIdx.x;
+  C v[kRowUnroll];
+  T f[kRowUnroll];
 #pragma unroll
-      for (int u = 0; u < kRowUnroll; ++u) {
-        const int i1 = b + u * blockDim.x;
-        if (i1 < N0) {
-          const int k1 = i1 - N0 / 2;
-          v[u] = src[k1 >= 0 ? k1 : nf0 + k1];
-          f[u] = fac0[i1];
-        }
-      }
+  for (int u = 0; u < kRowUnroll; ++u) {
+    const int i1 = b + u * blockDim.x;
+    if (i1 < m.N0) {
+      const int k1 = i1 - h0;
+      v[u] = src[AMPLIFY ? i1 : (k1 >= 0 ? k1 : m.nf0 + k1)];
+      f[u] = m.fac0[i1];
+    }
+  }
 #pragma unroll
-      for (int u = 0; u < kRowUnroll; ++u) {
-        const int i1 = b + u * blockDim.x;
-        if (i1 < N0) {
-          const T g = f[u] * f23;
-          C o;
-          o.x = v[u].x * g;
-          o.y = v[u].y * g;
-          dst[i1] = o;
-        }
-      }
+  for (int u = 0; u < kRowUnroll; ++u) {
+    const int i1 = b + u * blockDim.x;
+    if (i1 < m.N0) {
+      const int k1 = i1 - h0;
+      const T g = f[u] * f23;
+      C o;
+      o.x = v[u].x * g;
+      o.y = v[u].y * g;
+      dst[AMPLIFY ? (k1 >= 0 ? k1 : m.nf0 + k1) : i1] = o;
     }
   }
 }
 
-static int row_grid(long long rows) {
-  long long cap = 152LL * 16;
-  return (int)(rows < cap ? (rows < 1 ? 1 : rows) : cap);
+template <typename T, bool AMPLIFY>
+static cudaError_t launch_mode_rows(int dim, const int nf[3], const int N[3], const cplx_t<T>* in,
+                                    cplx_t<T>* out, const T* fac0, const T* fac1, const T* fac2, int ntr,
+                                    cudaStream_t s) {
+  ModeRows<T> m;
+  m.nf0 = nf[0];
+  m.nf1 = nf[1];
+  m.nf2 = nf[2];
+  m.N0 = N[0];
+  m.N1 = dim > 1 ? N[1] : 1;
+  m.N2 = dim > 2 ? N[2] : 1;
+  m.Nf = (long long)nf[0] * nf[1] * nf[2];
+  m.Nm = (long long)N[0] * N[1] * N[2];
+  m.nrows = m.N1 * m.N2;
+  m.fac0 = fac0;
+  m.fac1 = fac1;
+  m.fac2 = fac2;
+  if (m.N0 <= 0 || m.nrows <= 0 || ntr <= 0) return cudaSuccess;
+  // tx: enough threads for a row in one pass, a multiple of 32, at most 256
+  const int per = (m.N0 + kRowUnroll - 1) / kRowUnroll;
+  const int tx = std::min(256, std::max(32, (per + 31) / 32 * 32));
+  const int ty = 256 / tx;
+  m.nchunks = (m.N0 + kRowUnroll * tx - 1) / (kRowUnroll * tx);
+  const long long blocks = (long long)((m.nrows + ty - 1) / ty) * m.nchunks;
+  if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+  for (int t0 = 0; t0 < ntr; t0 += 65535) {
+    const int nt = std::min(ntr - t0, 65535);
+    const size_t off = (size_t)t0 * (AMPLIFY ? m.Nm : m.Nf), offo = (size_t)t0 * (AMPLIFY ? m.Nf : m.Nm);
+    dim3 grid((unsigned)blocks, nt);
+    dim3 block(tx, ty);
+    switch (dim) {
+      case 1: k_mode_rows<T, 1, AMPLIFY><<<grid, block, 0, s>>>(m, in + off, out + offo); break;
+      case 2: k_mode_rows<T, 2, AMPLIFY><<<grid, block, 0, s>>>(m, in + off, out + offo); break;
+      default: k_mode_rows<T, 3, AMPLIFY><<<grid, block, 0, s>>>(m, in + off, out + offo); break;
+    }
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 template <typename T>
 cudaError_t launch_deconvolve(int dim, const int nf[3], const int N[3], const cplx_t<T>* fw,
                               cplx_t<T>* fk, const T* fac0, const T* fac1, const T* fac2, int ntr,
                               cudaStream_t s) {
-  long long rows = (long long)N[1] * N[2] * ntr;
-  k_deconvolve<T><<<row_grid(rows), 256, 0, s>>>(dim, nf[0], nf[1], nf[2], N[0], N[1], N[2], fw, fk,
-                                                 fac0, fac1, fac2, ntr);
-  return cudaGetLastError();
+  return launch_mode_rows<T, false>(dim, nf, N, fw, fk, fac0, fac1, fac2, ntr, s);
 }
 
 // Type-2 amplification into a grid whose padding is already zero (the FFT
-// then runs out of place): only the mode cells are written, one block row per
-// (k2, k3) mode row, threads over k1 -- the mirror of k_deconvolve.
-template <typename T>
-__global__ void __launch_bounds__(256)
-k_amplify_modes(int dim, int nf0, int nf1, int nf2, int N0, int N1, int N2, cplx_t<T>* __restrict__ fw,
-                const cplx_t<T>* __restrict__ fk, const T* __restrict__ fac0, const T* __restrict__ fac1,
-                const T* __restrict__ fac2, int ntr) {
-  using C = cplx_t<T>;
-  const long long Nf = (long long)nf0 * nf1 * nf2;
-  const long long Nm = (long long)N0 * N1 * N2;
-  const int nrows = N1 * N2;
-  for (int r = blockIdx.x; r < nrows * ntr; r += gridDim.x) {
-    const int t = r / nrows;
-    const int rr = r - t * nrows;
-    const int i2 = rr % N1, i3 = rr / N1;
-    const int k2 = i2 - N1 / 2, k3 = i3 - N2 / 2;
-    const int w2 = k2 >= 0 ? k2 : nf1 + k2;
-    const int w3 = k3 >= 0 ? k3 : nf2 + k3;
-    T f23 = T(1);
-    if (dim > 1) f23 = fac1[i2];
-    if (dim > 2) f23 *= fac2[i3];
-    C* dst = fw + (size_t)t * Nf + ((size_t)w3 * nf1 + w2) * nf0;
-    const C* src = fk + (size_t)t * Nm + ((size_t)i3 * N1 + i2) * N0;
-    for (int b = threadIdx.x; b < N0; b += kRowUnroll * blockDim.x) {
-      C v[kRowUnroll];
-      T f[kRowUnroll];
-#pragma unroll
-      for (int u = 0; u < kRowUnroll; ++u) {
-        const int i1 = b + u * blockDim.x;
-        if (i1 < N0) {
-          v[u] = src[i1];
-          f[u] = fac0[i1];
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < kRowUnroll; ++u) {
-        const int i1 = b + u * blockDim.x;
-        if (i1 < N0) {
-          const int k1 = i1 - N0 / 2;
-          const T g = f[u] * f23;
-          C o;
-          o.x = v[u].x * g;
-          o.y = v[u].y * g;
-          dst[k1 >= 0 ? k1 : nf0 + k1] = o;
-        }
-      }
-    }
-  }
-}
-
+// then runs out of place): only the mode cells are written.
 template <typename T>
 cudaError_t launch_amplify_modes(int dim, const int nf[3], const int N[3], cplx_t<T>* fw,
                                  const cplx_t<T>* fk, const T* fac0, const T* fac1, const T* fac2,
                                  int ntr, cudaStream_t s) {
-  const long long rows = (long long)N[1] * N[2] * ntr;
-  const int grid = (int)std::min<long long>(std::max<long long>(rows, 1), 152LL * 32);
-  k_amplify_modes<T><<<grid, 256, 0, s>>>(dim, nf[0], nf[1], nf[2], N[0], N[1], N[2], fw, fk, fac0,
-                                          fac1, fac2, ntr);
-  return cudaGetLastError();
+  return launch_mode_rows<T, true>(dim, nf, N, fk, fw, fac0, fac1, fac2, ntr, s);
 }
+
 template cudaError_t launch_amplify_modes<float>(int, const int*, const int*, cplx_t<float>*,
                                                  const cplx_t<float>*, const float*, const float*,
                                                  const float*, int, cudaStream_t);

@@ -31,6 +31,10 @@
 namespace cfg {
 
 constexpr int kSpreadThreads = 256;
+// Threads of a k_interp_sm block, and its blocks per SM at the FP32
+// register bound (40 registers a thread for ns <= 9).
+constexpr int kInterpThreads = 256;
+constexpr int kInterpBlocksF32 = 6 * 256 / kInterpThreads;
 
 // Subproblem header shared by the shared-memory kernels.
 struct SubTile {
@@ -534,7 +538,7 @@ struct InterpPoint {
 // wait: evaluated before it, the rows stay live across the wait and the FP32
 // kernels spill at the 40-register bound (measured 3.5% slower).
 template <typename T, int DIM, int NS>
-__global__ void __launch_bounds__(kSpreadThreads, sizeof(T) == 4 ? (NS <= 9 ? 6 : 4) : 1)  // FP32 ns <= 9: 40 regs, 6 blocks/SM
+__global__ void __launch_bounds__(kInterpThreads, sizeof(T) == 4 ? (NS <= 9 ? kInterpBlocksF32 : kInterpBlocksF32 * 2 / 3) : 1)
 k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) {
   using C = cplx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1136,7 +1140,7 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     dim3 grid(a.bins.nsub, a.ntr);
     if (wc) k_interp_sm_wc<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
-    else k_interp_sm<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a, gmap, tma);
+    else k_interp_sm<T, DIM, NS><<<grid, kInterpThreads, sm, s>>>(a, gmap, tma);
   }
   return cudaGetLastError();
 }
