@@ -461,9 +461,19 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   if (p->method == 2) p->sort = 1;
 
   const int obin[3] = {p->opts.gpu_obinsizex, p->opts.gpu_obinsizey, p->opts.gpu_obinsizez};
+  p->spread_only = p->opts.gpu_spreadinterponly != 0;
   for (int k = 0; k < dim; ++k) {
     if (bins_from_obin && obin[k] <= 0) return CUFINUFFT_ERR_ARG;
-    p->nf[k] = set_nf_type12(p->N[k], p->opts.upsampfac, p->sp.ns, m, bins_from_obin ? obin[k] : 1);
+    if (p->spread_only) {
+      // spread/interpolation only: nmodes is the caller's grid itself; it
+      // must hold a kernel's support twice (as set_nf_type12's grids do),
+      // and for method 4 whole output bins
+      if (p->N[k] < 2 * p->sp.ns) return CUFINUFFT_ERR_ARG;
+      if (bins_from_obin && p->N[k] % obin[k] != 0) return CUFINUFFT_ERR_ARG;
+      p->nf[k] = p->N[k];
+    } else {
+      p->nf[k] = set_nf_type12(p->N[k], p->opts.upsampfac, p->sp.ns, m, bins_from_obin ? obin[k] : 1);
+    }
   }
   const int bsz[3] = {p->opts.gpu_binsizex, p->opts.gpu_binsizey, p->opts.gpu_binsizez};
   for (int k = 0; k < 3; ++k) {
@@ -497,12 +507,27 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   CFG_CUDA(cudaMallocHost(&p->h_total, sizeof(int)));
 
   const long long Nf = grid_cells(p);
-  CFG_CUDA(cudaMalloc(&p->fw, sizeof(cplx_t<T>) * (size_t)Nf * p->maxbatch));
-  for (int k = 0; k < dim; ++k) CFG_CUDA(cudaMalloc(&p->fac[k], sizeof(T) * (size_t)p->N[k]));
   CFG_CUDA(cudaMalloc(&p->count, sizeof(int) * (size_t)p->nbins));
   CFG_CUDA(cudaMalloc(&p->start, sizeof(int) * ((size_t)p->nbins + 1)));
   CFG_CUDA(cudaMalloc(&p->sub_start, sizeof(int) * ((size_t)p->nbins + 1)));
   CFG_CUDA(cudaMalloc(&p->scan_tmp, sizeof(int) * (size_t)scan_tmp_ints(p->nbins)));
+  if (p->spread_only) {
+    // no grid, FFT or kernel Fourier series: execute spreads into / reads
+    // from the caller's fk
+    if (p->opts.gpu_kerevalmeth == 1) {
+      const int deg = horner_degree<T>(p->sp.ns);
+      std::vector<double> cd = horner_fit(p->sp, deg);
+      p->horner.assign(cd.begin(), cd.end());
+      CFG_CUDA(cudaMalloc(&p->horner_d, sizeof(T) * p->horner.size()));
+      CFG_CUDA(cudaMemcpyAsync(p->horner_d, p->horner.data(), sizeof(T) * p->horner.size(),
+                               cudaMemcpyHostToDevice, p->stream));
+    }
+    CFG_CUDA(cudaStreamSynchronize(p->stream));
+    p->planned = true;
+    return 0;
+  }
+  CFG_CUDA(cudaMalloc(&p->fw, sizeof(cplx_t<T>) * (size_t)Nf * p->maxbatch));
+  for (int k = 0; k < dim; ++k) CFG_CUDA(cudaMalloc(&p->fac[k], sizeof(T) * (size_t)p->N[k]));
 
   int e = 0;
   if (use_line_fft(p)) {
@@ -778,6 +803,24 @@ static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
     if (p->timing)
       for (int k = 0; k < 4; ++k) ev[k] = take_event(p);
     mark(p, ev[0]);
+    if (p->spread_only) {
+      // the caller's fk is the fine grid (nf = nmodes): spread into it or
+      // interpolate from it, no FFT and no deconvolution
+      mark(p, ev[1]);
+      mark(p, ev[2]);
+      if (p->type == 1) {
+        a.c_in = c + (size_t)b0 * p->M;
+        a.fw = fk + (size_t)b0 * Nf;
+        CFG_CUDA(cudaMemsetAsync(a.fw, 0, sizeof(cplx_t<T>) * (size_t)Nf * B, p->stream));
+        CFG_CUDA(run_spread(p, a));
+      } else {
+        a.fw_in = fk + (size_t)b0 * Nf;
+        a.c_out = c + (size_t)b0 * p->M;
+        CFG_CUDA(run_interp(p, a));
+      }
+      mark(p, ev[3]);
+      continue;
+    }
     if (p->type == 1) {
       a.c_in = c + (size_t)b0 * p->M;
       a.fw = p->fw;
@@ -1029,7 +1072,7 @@ static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub)
 // Device time (ms) of the plan's spread (type 1) or interp (type 2) stage for
 // one batch, median of `reps` runs after one warm-up, on synthetic values.
 template <typename T>
-static int time_stage(Plan<T>* p, cplx_t<T>* scratch, int reps, float* ms) {
+static int time_stage(Plan<T>* p, cplx_t<T>* scratch, cplx_t<T>* grid, int reps, float* ms) {
   SpreadArgs<T> a = spread_args(p);
   a.ntr = p->maxbatch;
   cudaEvent_t e0, e1;
@@ -1040,10 +1083,10 @@ static int time_stage(Plan<T>* p, cplx_t<T>* scratch, int reps, float* ms) {
     CFG_CUDA(cudaEventRecord(e0, p->stream));
     if (p->type == 1) {
       a.c_in = scratch;
-      a.fw = p->fw;
+      a.fw = grid;
       CFG_CUDA(run_spread(p, a));
     } else {
-      a.fw_in = p->fw2 ? p->fw2 : p->fw;
+      a.fw_in = grid;
       a.c_out = scratch;
       CFG_CUDA(run_interp(p, a));
     }
@@ -1113,31 +1156,41 @@ static int autotune_impl(Plan<T>* p, cufinufft_tune_entry* out, int max_out, int
   if (p->M == 0) return 0;
   cplx_t<T>* scratch = nullptr;
   CFG_CUDA(cudaMalloc(&scratch, sizeof(cplx_t<T>) * (size_t)p->M * p->maxbatch));
+  // the grid the stage writes (type 1) or reads (type 2): the plan's own, or
+  // a temporary one for a spread/interpolation-only plan (its grid is the
+  // caller's); never the type-2 FFT input, whose padding must stay zero
+  const size_t grid_bytes = sizeof(cplx_t<T>) * (size_t)grid_cells(p) * p->maxbatch;
+  cplx_t<T>* grid = p->type == 1 ? p->fw : (p->fw2 ? p->fw2 : p->fw);
+  cplx_t<T>* tmp_grid = nullptr;
+  if (p->spread_only) {
+    if (cudaMalloc(&tmp_grid, grid_bytes) != cudaSuccess) {
+      cudaFree(scratch);
+      return CUFINUFFT_ERR_ALLOC;
+    }
+    grid = tmp_grid;
+  }
   // nonzero synthetic strengths/values (a zero tile would be skipped)
   CFG_CUDA(cudaMemsetAsync(scratch, 0x3f, sizeof(cplx_t<T>) * (size_t)p->M * p->maxbatch, p->stream));
-  if (p->type == 2)
-    CFG_CUDA(cudaMemsetAsync(p->fw2 ? p->fw2 : p->fw, 0x3f,
-                             sizeof(cplx_t<T>) * (size_t)grid_cells(p) * p->maxbatch,
-                             p->stream));
+  if (p->type == 2) CFG_CUDA(cudaMemsetAsync(grid, 0x3f, grid_bytes, p->stream));
   int best = -1;
   for (size_t i = 0; i < cand.size(); ++i) {
     if (cand[i].ms == -2.f) continue;  // not runnable for this plan
     int bs[3] = {cand[i].binsizex, cand[i].binsizey, cand[i].binsizez};
     int e = set_layout_impl(p, cand[i].method, bs, cand[i].maxsubprobsize);
     if (e) continue;
-    if (p->type == 1)
-      CFG_CUDA(cudaMemsetAsync(p->fw, 0, sizeof(cplx_t<T>) * (size_t)grid_cells(p) * p->maxbatch,
-                               p->stream));
+    if (p->type == 1) CFG_CUDA(cudaMemsetAsync(grid, 0, grid_bytes, p->stream));
     float ms = 0;
-    e = time_stage(p, scratch, 3, &ms);
+    e = time_stage(p, scratch, grid, 3, &ms);
     if (e) {
       cudaFree(scratch);
+      cudaFree(tmp_grid);
       return e;
     }
     cand[i].ms = ms;
     if (best < 0 || ms < cand[best].ms) best = (int)i;
   }
   cudaFree(scratch);
+  cudaFree(tmp_grid);
   if (best < 0) return CUFINUFFT_ERR_GENERIC;
   int bs[3] = {cand[best].binsizex, cand[best].binsizey, cand[best].binsizez};
   int e = set_layout_impl(p, cand[best].method, bs, cand[best].maxsubprobsize);

@@ -91,6 +91,7 @@ static int batch_make(Batch<T>* b, int nplans, Plan<T>** plans) {
     if (p->type != b->type || p->dim != b->dim || p->sp.ns != b->ns || p->device != b->device)
       return CUFINUFFT_ERR_ARG;  // one type, dimension, kernel width and device per batch
     if (p->opts.gpu_kerevalmeth != 0) return CUFINUFFT_ERR_ARG;
+    if (p->spread_only) return CUFINUFFT_ERR_ARG;  // the batch runs whole transforms
     b->plans.push_back(p);
   }
   CFG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));

@@ -34,6 +34,7 @@ template <typename T> struct Plan {
   int device = 0;
   int M = 0, nsub = 0;
   bool planned = false, pts_set = false;
+  bool spread_only = false;  // gpu_spreadinterponly: fk is the fine grid, no FFT/deconvolution
   cudaStream_t own = nullptr, stream = nullptr;
   cufftHandle fft = 0, fft_rem = 0;
   bool have_fft = false, have_fft_rem = false;

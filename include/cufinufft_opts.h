@@ -26,9 +26,12 @@ typedef struct cufinufft_opts {
   int gpu_nstreams;          /* accepted for ABI parity, unused            */
   int gpu_kerevalmeth;       /* 0: exp(beta*sqrt(1-c x^2)), 1: piecewise
                                 polynomial (Horner) fitted at plan time    */
-  int gpu_spreadinterponly;  /* accepted for ABI parity; execute() always
-                                runs the full transform, as the reference's
-                                execute does                               */
+  int gpu_spreadinterponly;  /* 1: spread/interpolate only -- nmodes is the
+                                fine grid itself (each >= 2 ns), execute()
+                                spreads c into fk (type 1) or interpolates
+                                fk to c (type 2), no FFT or deconvolution;
+                                the reference sets this flag in its
+                                spread/interp tests (test/spread2d_test.cu:80) */
   int gpu_device_id;         /* CUDA device the plan lives on              */
 } cufinufft_opts;
 

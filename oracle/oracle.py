@@ -142,7 +142,7 @@ class OraclePlan:
     """
 
     def __init__(self, nufft_type: int, modes, iflag: int, tol: float, single: bool,
-                 gpu_method: int = 0, obin: tuple = (8, 8, 8)):
+                 gpu_method: int = 0, obin: tuple = (8, 8, 8), spreadinterponly: bool = False):
         self.type = int(nufft_type)
         self.modes = tuple(int(m) for m in modes)
         self.dim = len(self.modes)
@@ -150,8 +150,14 @@ class OraclePlan:
         ier, self.ns, self.beta, self.c = setup_spreader(tol, single)
         if ier > 1:
             raise ValueError(f"setup_spreader error {ier}")
-        self.nf = tuple(set_nf_type12(m, self.ns, gpu_method, obin[d])
-                        for d, m in enumerate(self.modes))
+        if spreadinterponly:
+            # the grid is the modes array itself (the reference's spread /
+            # interp tests set gpu_spreadinterponly and pass nf directly,
+            # test/spread2d_test.cu:80,133)
+            self.nf = self.modes
+        else:
+            self.nf = tuple(set_nf_type12(m, self.ns, gpu_method, obin[d])
+                            for d, m in enumerate(self.modes))
         self.ker = [fseries(nf, self.ns, self.beta, self.c) for nf in self.nf]
 
     def _pts(self, x, y, z):
