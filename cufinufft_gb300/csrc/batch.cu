@@ -7,47 +7,85 @@
 
 namespace cfg {
 
-// Fork: every side stream waits for the work queued so far on b->stream.
+// An event of the recorded sequence (a fresh one per record or wait pair,
+// so every dependency of the captured graph is explicit).
 template <typename T>
-static int fork_sides(Batch<T>* b) {
-  CFG_CUDA(cudaEventRecord(b->fork_ev, b->stream));
-  for (int k = 0; k < Batch<T>::kSide; ++k) CFG_CUDA(cudaStreamWaitEvent(b->side[k], b->fork_ev, 0));
-  return 0;
-}
-// Join: b->stream waits for everything queued on the side streams.
-template <typename T>
-static int join_sides(Batch<T>* b) {
-  for (int k = 0; k < Batch<T>::kSide; ++k) {
-    CFG_CUDA(cudaEventRecord(b->join_ev[k], b->side[k]));
-    CFG_CUDA(cudaStreamWaitEvent(b->stream, b->join_ev[k], 0));
+static cudaError_t next_event(Batch<T>* b, cudaEvent_t* ev) {
+  if (b->evnext == b->evpool.size()) {
+    cudaEvent_t e;
+    const cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (r != cudaSuccess) return r;
+    b->evpool.push_back(e);
   }
+  *ev = b->evpool[b->evnext++];
+  return cudaSuccess;
+}
+
+// `to` waits for everything queued so far on `from`.
+template <typename T>
+static cudaError_t follow(Batch<T>* b, cudaStream_t from, cudaStream_t to) {
+  cudaEvent_t e;
+  cudaError_t r = next_event(b, &e);
+  if (r == cudaSuccess) r = cudaEventRecord(e, from);
+  if (r == cudaSuccess) r = cudaStreamWaitEvent(to, e, 0);
+  return r;
+}
+
+// Spread/interp kernels of one group: side[0] and side[1] fork from and join
+// back into b->stream.
+template <typename T>
+static int group_spreadinterp(Batch<T>* b, const BatchGroup& g) {
+  if (g.t1 <= g.t0 && g.b1 <= g.b0) return 0;
+  CFG_CUDA(follow(b, b->stream, b->side[0]));
+  CFG_CUDA(follow(b, b->stream, b->side[1]));
+  CFG_CUDA(batch_spreadinterp(b, g));
+  CFG_CUDA(follow(b, b->side[0], b->stream));
+  CFG_CUDA(follow(b, b->side[1], b->stream));
   return 0;
 }
 
-// The per-plan FFTs, spread over b->stream and the side streams.
+// FFT stream of plan i: the kFftSide FFT streams in turn.
 template <typename T>
-static int batch_ffts(Batch<T>* b) {
-  const int n = (int)b->plans.size();
-  int e = fork_sides(b);
-  if (e) return e;
-  for (int i = 0; i < n; ++i) {
-    const int br = i % (Batch<T>::kSide + 1);
-    cudaStream_t st = br == 0 ? b->stream : b->side[br - 1];
-    CFG_CUFFT(cufftSetStream(b->fft[i], st));
+static cudaStream_t fft_stream(Batch<T>* b, int i) {
+  return b->side[2 + i % Batch<T>::kFftSide];
+}
+
+// The FFTs of plans [p0, p1), each on its plan's FFT stream after the work
+// queued so far on b->stream; returns (in *joined) the stream of plan p0,
+// made to wait for all of them.
+template <typename T>
+static int group_ffts(Batch<T>* b, int p0, int p1, cudaStream_t* joined) {
+  const int used = std::min(p1 - p0, Batch<T>::kFftSide);
+  for (int i = p0; i < p0 + used; ++i) {
+    CFG_CUDA(follow(b, b->stream, fft_stream(b, i)));
+    b->fft_used |= 1u << (i % Batch<T>::kFftSide);
+  }
+  for (int i = p0; i < p1; ++i) {
+    CFG_CUFFT(cufftSetStream(b->fft[i], fft_stream(b, i)));
     CFG_CUFFT(fft_exec(b->fft[i], b->fw[i], b->plans[i]->iflag));
   }
-  return join_sides(b);
+  cudaStream_t a = fft_stream(b, p0);
+  for (int i = p0 + 1; i < p0 + used; ++i) CFG_CUDA(follow(b, fft_stream(b, i), a));
+  *joined = a;
+  return 0;
 }
 
-// Records the whole batch sequence on b->stream (capture or direct); the
-// method-1 and method-2 spread/interp kernels run on parallel branches, and
-// the FFTs on kSide + 1 branches.
+static int row_blocks(long long rows) {
+  return (int)std::min<long long>(std::max<long long>(rows, 1), 152LL * 16);
+}
+
+// Records the whole batch sequence on b->stream (capture or direct).
+// Type 1 runs its groups as a pipeline: group g's spread kernels on b->stream
+// (and side[0], side[1]); then its FFTs on the FFT streams and its
+// deconvolution behind them while group g + 1 is spread.  Type 2 amplifies
+// every plan, runs every FFT and interpolates, one stage after the other.
 template <typename T>
 static int batch_record(Batch<T>* b) {
   const int n = (int)b->plans.size();
+  b->evnext = 0;
+  b->fft_used = 0;
   CFG_CUDA(cudaMemcpyAsync(b->d_desc, b->h_desc, sizeof(BatchDesc<T>) * n, cudaMemcpyHostToDevice,
                            b->stream));
-  const int rgrid = (int)std::min<long long>(std::max<long long>(b->nrows, 1), 152LL * 16);
   int e = 0;
   if (b->type == 1) {
     for (int i = 0; i < n; ++i) {
@@ -55,25 +93,76 @@ static int batch_record(Batch<T>* b) {
       CFG_CUDA(cudaMemsetAsync(b->fw[i], 0, sizeof(cplx_t<T>) * (size_t)grid_cells(p) * p->ntransf,
                                b->stream));
     }
-    if (b->ntasks > 0 || b->nblocks > 0) {
-      if ((e = fork_sides(b))) return e;
-      CFG_CUDA(batch_spreadinterp(b));
-      if ((e = join_sides(b))) return e;
+    for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+      const BatchGroup& g = b->groups[gi];
+      if ((e = group_spreadinterp(b, g))) return e;
+      cudaStream_t a = nullptr;
+      if ((e = group_ffts(b, g.p0, g.p1, &a))) return e;
+      if (g.r1 > g.r0) {
+        k_batch_deconvolve<T><<<row_blocks(g.r1 - g.r0), 256, 0, a>>>(b->d_desc, n, g.r0, g.r1, b->dim);
+        CFG_CUDA(cudaGetLastError());
+      }
     }
-    if ((e = batch_ffts(b))) return e;
-    k_batch_deconvolve<T><<<rgrid, 256, 0, b->stream>>>(b->d_desc, n, b->nrows, b->dim);
-    CFG_CUDA(cudaGetLastError());
+    // join the FFT streams this sequence used (an unused one never joined
+    // the capture)
+    for (int k = 0; k < Batch<T>::kFftSide; ++k)
+      if (b->fft_used & (1u << k)) CFG_CUDA(follow(b, b->side[2 + k], b->stream));
   } else {
-    k_batch_amplify<T><<<rgrid, 256, 0, b->stream>>>(b->d_desc, n, b->nrows, b->dim);
+    const BatchGroup all = {0, n, 0, b->ntasks, 0, b->nblocks, 0, b->nrows};
+    k_batch_amplify<T><<<row_blocks(b->nrows), 256, 0, b->stream>>>(b->d_desc, n, 0, b->nrows, b->dim);
     CFG_CUDA(cudaGetLastError());
-    if ((e = batch_ffts(b))) return e;
-    if (b->ntasks > 0 || b->nblocks > 0) {
-      if ((e = fork_sides(b))) return e;
-      CFG_CUDA(batch_spreadinterp(b));
-      if ((e = join_sides(b))) return e;
-    }
+    cudaStream_t a = nullptr;
+    if ((e = group_ffts(b, 0, n, &a))) return e;
+    CFG_CUDA(follow(b, a, b->stream));
+    if ((e = group_spreadinterp(b, all))) return e;
   }
   return 0;
+}
+
+// Type-1 groups: consecutive plans cut where the running tap count (M ntr
+// ns^d per plan) crosses k / kBatchGroups of the total, so each group's spread
+// is about as long and its FFTs overlap the next group's spreading.
+constexpr int kBatchGroups = 4;
+
+template <typename T>
+static void make_groups(Batch<T>* b) {
+  const int n = (int)b->plans.size();
+  b->groups.clear();
+  auto group_of = [&](int p0, int p1) {
+    BatchGroup g;
+    g.p0 = p0;
+    g.p1 = p1;
+    g.t0 = b->h_desc[p0].task0;
+    g.b0 = b->h_desc[p0].blk0;
+    g.r0 = b->h_desc[p0].row0;
+    g.t1 = p1 < n ? b->h_desc[p1].task0 : b->ntasks;
+    g.b1 = p1 < n ? b->h_desc[p1].blk0 : b->nblocks;
+    g.r1 = p1 < n ? b->h_desc[p1].row0 : b->nrows;
+    return g;
+  };
+  if (b->type != 1) {
+    b->groups.push_back(group_of(0, n));
+    return;
+  }
+  std::vector<double> w(n);
+  double total = 0;
+  for (int i = 0; i < n; ++i) {
+    const Plan<T>* p = b->plans[i];
+    w[i] = (double)p->M * p->ntransf * std::pow((double)p->sp.ns, p->dim) + 1.0;
+    total += w[i];
+  }
+  const int G = std::min(n, kBatchGroups);
+  double acc = 0;
+  int p0 = 0;
+  for (int i = 0; i < n; ++i) {
+    acc += w[i];
+    const int k = (int)b->groups.size() + 1;
+    if (i + 1 < n && k < G && acc >= total * k / G) {
+      b->groups.push_back(group_of(p0, i + 1));
+      p0 = i + 1;
+    }
+  }
+  b->groups.push_back(group_of(p0, n));
 }
 
 template <typename T>
@@ -96,11 +185,8 @@ static int batch_make(Batch<T>* b, int nplans, Plan<T>** plans) {
   }
   CFG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   CFG_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
-  CFG_CUDA(cudaEventCreateWithFlags(&b->fork_ev, cudaEventDisableTiming));
-  for (int k = 0; k < Batch<T>::kSide; ++k) {
+  for (int k = 0; k < Batch<T>::kSide; ++k)
     CFG_CUDA(cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
-    CFG_CUDA(cudaEventCreateWithFlags(&b->join_ev[k], cudaEventDisableTiming));
-  }
   CFG_CUDA(cudaMallocHost(&b->h_desc, sizeof(BatchDesc<T>) * nplans));
   CFG_CUDA(cudaMalloc(&b->d_desc, sizeof(BatchDesc<T>) * nplans));
   long long task = 0, row = 0, blk = 0;
@@ -174,6 +260,7 @@ static int batch_make(Batch<T>* b, int nplans, Plan<T>** plans) {
   b->ntasks = task;
   b->nrows = row;
   b->nblocks = blk;
+  make_groups(b);
   return 0;
 }
 

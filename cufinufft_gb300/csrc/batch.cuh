@@ -75,7 +75,7 @@ __device__ __forceinline__ T batch_tap(T d, int j, const BatchDesc<T>& P) {
 // point chunks of every plan.
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
-k_batch_spread(const BatchDesc<T>* D, int nplans, long long ntasks) {
+k_batch_spread(const BatchDesc<T>* D, int nplans, long long task_begin, long long task_end) {
   using C = cplx_t<T>;
   constexpr int L = spread_lanes<NS>();
   constexpr int PPW = 32 / L;
@@ -86,7 +86,7 @@ k_batch_spread(const BatchDesc<T>* D, int nplans, long long ntasks) {
   const int jj = tap ? j : 0;
   const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long task = wid; task < ntasks; task += nw) {
+  for (long long task = task_begin + wid; task < task_end; task += nw) {
     const BatchDesc<T>& P = D[find_plan(D, nplans, task, 0)];
     const long long pl = (task - P.task0) * PPW + g;
     const bool valid = g < PPW && pl < P.M;
@@ -121,7 +121,7 @@ k_batch_spread(const BatchDesc<T>* D, int nplans, long long ntasks) {
 // Interpolation, warp-cooperative (as k_interp_gm_wc), over every plan.
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
-k_batch_interp(const BatchDesc<T>* D, int nplans, long long ntasks) {
+k_batch_interp(const BatchDesc<T>* D, int nplans, long long task_begin, long long task_end) {
   using C = cplx_t<T>;
   constexpr int L = lanes_per_point<NS>();
   constexpr int PPW = 32 / L;
@@ -132,7 +132,7 @@ k_batch_interp(const BatchDesc<T>* D, int nplans, long long ntasks) {
   const int jj = tap ? j : 0;
   const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long task = wid; task < ntasks; task += nw) {
+  for (long long task = task_begin + wid; task < task_end; task += nw) {
     const BatchDesc<T>& P = D[find_plan(D, nplans, task, 0)];
     const long long pl = (task - P.task0) * PPW + g;
     const bool valid = pl < P.M;
@@ -184,9 +184,9 @@ k_batch_interp(const BatchDesc<T>* D, int nplans, long long ntasks) {
 // k_deconvolve): row task r of plan P is (t, i2, i3).
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_batch_deconvolve(const BatchDesc<T>* D, int nplans, long long nrows, int dim) {
+k_batch_deconvolve(const BatchDesc<T>* D, int nplans, long long row_begin, long long row_end, int dim) {
   using C = cplx_t<T>;
-  for (long long r = blockIdx.x; r < nrows; r += gridDim.x) {
+  for (long long r = row_begin + blockIdx.x; r < row_end; r += gridDim.x) {
     const BatchDesc<T>& P = D[find_plan(D, nplans, r, 1)];
     const long long rr0 = r - P.row0;
     const long long per = (long long)P.N[1] * P.N[2];
@@ -218,9 +218,9 @@ k_batch_deconvolve(const BatchDesc<T>* D, int nplans, long long nrows, int dim) 
 // k_amplify), writing every cell.
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_batch_amplify(const BatchDesc<T>* D, int nplans, long long nrows, int dim) {
+k_batch_amplify(const BatchDesc<T>* D, int nplans, long long row_begin, long long row_end, int dim) {
   using C = cplx_t<T>;
-  for (long long r = blockIdx.x; r < nrows; r += gridDim.x) {
+  for (long long r = row_begin + blockIdx.x; r < row_end; r += gridDim.x) {
     const BatchDesc<T>& P = D[find_plan(D, nplans, r, 1)];
     const long long rr0 = r - P.row0;
     const long long per = (long long)P.nf[1] * P.nf[2];
@@ -267,14 +267,14 @@ k_batch_amplify(const BatchDesc<T>* D, int nplans, long long nrows, int dim) {
 // of every method-2 plan; one block per (subproblem, transform).
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
-k_batch_spread_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
+k_batch_spread_sm(const BatchDesc<T>* D, int nplans, long long blk_begin, long long blk_end) {
   using C = cplx_t<T>;
   constexpr int L = spread_lanes<NS>();
   constexpr int PPW = 32 / L;
   constexpr int NY = DIM > 1 ? NS : 1;
   constexpr int NZ = DIM > 2 ? NS : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  for (long long task = blockIdx.x; task < nblocks; task += gridDim.x) {
+  for (long long task = blk_begin + blockIdx.x; task < blk_end; task += gridDim.x) {
     const BatchDesc<T>& P = D[find_plan(D, nplans, task, 2)];
     const long long local = task - P.blk0;
     const int t = (int)(local / P.bins.nsub);
@@ -334,9 +334,9 @@ k_batch_spread_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
 // k_batch_spread_sm.
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
-k_batch_spread_run(const BatchDesc<T>* D, int nplans, long long nblocks) {
+k_batch_spread_run(const BatchDesc<T>* D, int nplans, long long blk_begin, long long blk_end) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  for (long long task = blockIdx.x; task < nblocks; task += gridDim.x) {
+  for (long long task = blk_begin + blockIdx.x; task < blk_end; task += gridDim.x) {
     const BatchDesc<T>& P = D[find_plan(D, nplans, task, 2)];
     const long long local = task - P.blk0;
     const int t = (int)(local / P.bins.nsub);
@@ -376,13 +376,13 @@ k_batch_spread_run(const BatchDesc<T>* D, int nplans, long long nblocks) {
 // plan.
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
-k_batch_interp_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
+k_batch_interp_sm(const BatchDesc<T>* D, int nplans, long long blk_begin, long long blk_end) {
   using C = cplx_t<T>;
   constexpr int NY = DIM > 1 ? NS : 1;
   constexpr int NZ = DIM > 2 ? NS : 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* tile = reinterpret_cast<C*>(smem_raw);
-  for (long long task = blockIdx.x; task < nblocks; task += gridDim.x) {
+  for (long long task = blk_begin + blockIdx.x; task < blk_end; task += gridDim.x) {
     const BatchDesc<T>& P = D[find_plan(D, nplans, task, 2)];
     const long long local = task - P.blk0;
     const int t = (int)(local / P.bins.nsub);
@@ -439,8 +439,20 @@ k_batch_interp_sm(const BatchDesc<T>* D, int nplans, long long nblocks) {
   }
 }
 
+// A run of consecutive plans [p0, p1) of a batch with its ranges of
+// point-chunk tasks [t0, t1), subproblem blocks [b0, b1) and mode/grid rows
+// [r0, r1) (the plans' task0/blk0/row0 prefix sums are monotone).
+struct BatchGroup {
+  int p0, p1;
+  long long t0, t1, b0, b1, r0, r1;
+};
+
 template <typename T> struct Batch {
   std::vector<Plan<T>*> plans;
+  std::vector<BatchGroup> groups;   // type 1: spread groups pipelined against FFTs
+  std::vector<cudaEvent_t> evpool;  // events of the recorded sequence
+  size_t evnext = 0;
+  unsigned fft_used = 0;            // FFT streams the recorded sequence used (bit k: side[2 + k])
   int type = 0, dim = 0, ns = 0, device = 0;
   std::vector<cplx_t<T>*> fw;
   std::vector<cufftHandle> fft;
@@ -450,12 +462,11 @@ template <typename T> struct Batch {
   size_t smem = 0;  // largest method-2 tile
   size_t smem_run = 0;  // largest cell-run footprint (0: no plan in that layout)
   cudaStream_t stream = nullptr;
-  // side streams: the method-2 spread/interp and the per-plan FFTs run on
-  // parallel branches of the captured graph
-  static constexpr int kSide = 4;
+  // side streams: the method-2 spread/interp kernels (0, 1) and the per-plan
+  // FFTs (2..7) run on parallel branches of the captured graph
+  static constexpr int kSide = 8;
+  static constexpr int kFftSide = kSide - 2;
   cudaStream_t side[kSide] = {};
-  cudaEvent_t fork_ev = nullptr;
-  cudaEvent_t join_ev[kSide] = {};
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   cudaEvent_t done = nullptr;
@@ -468,17 +479,16 @@ inline void batch_release(Batch<T>* b) {
   if (b->graph) cudaGraphDestroy(b->graph);
   for (cufftHandle h : b->fft) cufftDestroy(h);
   for (auto* p : b->fw) cudaFree(p);
+  for (cudaEvent_t e : b->evpool) cudaEventDestroy(e);
+  b->evpool.clear();
+  b->groups.clear();
   cudaFree(b->d_desc);
   if (b->h_desc) cudaFreeHost(b->h_desc);
   if (b->done) cudaEventDestroy(b->done);
-  if (b->fork_ev) cudaEventDestroy(b->fork_ev);
   for (int k = 0; k < Batch<T>::kSide; ++k) {
-    if (b->join_ev[k]) cudaEventDestroy(b->join_ev[k]);
     if (b->side[k]) cudaStreamDestroy(b->side[k]);
-    b->join_ev[k] = nullptr;
     b->side[k] = nullptr;
   }
-  b->fork_ev = nullptr;
   if (b->stream) cudaStreamDestroy(b->stream);
   b->gexec = nullptr;
   b->graph = nullptr;
@@ -490,45 +500,48 @@ inline void batch_release(Batch<T>* b) {
   b->stream = nullptr;
 }
 
+// The multi-plan spread/interp kernels over one group's task ranges:
+// method-1 chunks on b->stream, method-2 (and cell-run) blocks on side[0] and
+// side[1].
 template <typename T, int DIM>
-inline cudaError_t batch_spreadinterp_dim(Batch<T>* b, int n, long long ntasks) {
+inline cudaError_t batch_spreadinterp_dim(Batch<T>* b, int n, const BatchGroup& gr) {
   constexpr int kMaxGrid = 152 * 32;
-  const int PPWmax = 1;
-  (void)PPWmax;
-  const long long warps = ntasks;
-  long long blocks = (warps * 32 + kSpreadThreads - 1) / kSpreadThreads;
+  const long long ntasks = gr.t1 - gr.t0, nblk = gr.b1 - gr.b0;
+  long long blocks = (ntasks * 32 + kSpreadThreads - 1) / kSpreadThreads;
   if (blocks > kMaxGrid) blocks = kMaxGrid;
   if (blocks < 1) blocks = 1;
   const int g = (int)blocks;
-  const int gb = (int)std::min<long long>(std::max<long long>(b->nblocks, 1), 152LL * 8);
+  const int gb = (int)std::min<long long>(std::max<long long>(nblk, 1), 152LL * 8);
   cudaError_t fe = cudaSuccess;
 #define CFG_BATCH_CASE(NSV)                                                                       \
   case NSV:                                                                                       \
     if (b->type == 1) {                                                                           \
       if (ntasks > 0)                                                                             \
-        k_batch_spread<T, DIM, NSV><<<g, kSpreadThreads, 0, b->stream>>>(b->d_desc, n, ntasks);  \
-      if (b->nblocks > 0) {                                                                       \
+        k_batch_spread<T, DIM, NSV><<<g, kSpreadThreads, 0, b->stream>>>(b->d_desc, n, gr.t0,    \
+                                                                         gr.t1);                  \
+      if (nblk > 0) {                                                                             \
         fe = prepare_smem(k_batch_spread_sm<T, DIM, NSV>, b->smem);                               \
         if (fe != cudaSuccess) return fe;                                                         \
         k_batch_spread_sm<T, DIM, NSV><<<gb, kSpreadThreads, b->smem, b->side[0]>>>(b->d_desc, n, \
-                                                                                  b->nblocks);   \
+                                                                                  gr.b0, gr.b1); \
         if constexpr (run_ok<DIM, NSV>()) {                                                       \
           if (b->smem_run > 0) {                                                                  \
             fe = prepare_smem(k_batch_spread_run<T, DIM, NSV>, b->smem_run);                      \
             if (fe != cudaSuccess) return fe;                                                     \
             k_batch_spread_run<T, DIM, NSV><<<gb, kSpreadThreads, b->smem_run, b->side[1]>>>(     \
-                b->d_desc, n, b->nblocks);                                                        \
+                b->d_desc, n, gr.b0, gr.b1);                                                      \
           }                                                                                       \
         }                                                                                         \
       }                                                                                           \
     } else {                                                                                      \
       if (ntasks > 0)                                                                             \
-        k_batch_interp<T, DIM, NSV><<<g, kSpreadThreads, 0, b->stream>>>(b->d_desc, n, ntasks);  \
-      if (b->nblocks > 0) {                                                                       \
+        k_batch_interp<T, DIM, NSV><<<g, kSpreadThreads, 0, b->stream>>>(b->d_desc, n, gr.t0,    \
+                                                                         gr.t1);                  \
+      if (nblk > 0) {                                                                             \
         fe = prepare_smem(k_batch_interp_sm<T, DIM, NSV>, b->smem);                               \
         if (fe != cudaSuccess) return fe;                                                         \
         k_batch_interp_sm<T, DIM, NSV><<<gb, kSpreadThreads, b->smem, b->side[0]>>>(b->d_desc, n, \
-                                                                                  b->nblocks);   \
+                                                                                  gr.b0, gr.b1); \
       }                                                                                           \
     }                                                                                             \
     break;
@@ -542,9 +555,9 @@ inline cudaError_t batch_spreadinterp_dim(Batch<T>* b, int n, long long ntasks) 
   return cudaGetLastError();
 }
 
-// Multi-plan spread/interp launch for one precision; instantiated in
-// batch_f.cu and batch_d.cu.
+// Multi-plan spread/interp launch over one group for one precision;
+// instantiated in batch_f.cu and batch_d.cu.
 template <typename T>
-cudaError_t batch_spreadinterp(Batch<T>* b);
+cudaError_t batch_spreadinterp(Batch<T>* b, const BatchGroup& g);
 
 }  // namespace cfg

@@ -821,7 +821,6 @@ __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   T* kvw = im + st.ntile + warp * 32 * KV;  // staged kernel values of a dense chunk
   C* cvw = reinterpret_cast<C*>(im + st.ntile + NWARP * 32 * KV) + warp * 32;
-  const int t = blockIdx.y;
   for (int i = threadIdx.x; i < 2 * st.ntile; i += blockDim.x) re[i] = T(0);
   __syncthreads();
   const int S = (((st.np + NWARP - 1) / NWARP) + 31) & ~31;
