@@ -863,6 +863,24 @@ static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
   return 0;
 }
 
+// Entry points for the batch (batch.cu): a plan's whole execute, and moving
+// a plan's work, cuFFT plans included, to another stream.
+template <typename T>
+int execute_plan(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
+  return execute_impl(p, c, fk);
+}
+template <typename T>
+int plan_use_stream(Plan<T>* p, cudaStream_t s) {
+  p->stream = s;
+  if (p->have_fft) CFG_CUFFT(cufftSetStream(p->fft, s));
+  if (p->have_fft_rem) CFG_CUFFT(cufftSetStream(p->fft_rem, s));
+  return 0;
+}
+template int execute_plan<float>(Plan<float>*, cplx_t<float>*, cplx_t<float>*);
+template int execute_plan<double>(Plan<double>*, cplx_t<double>*, cplx_t<double>*);
+template int plan_use_stream<float>(Plan<float>*, cudaStream_t);
+template int plan_use_stream<double>(Plan<double>*, cudaStream_t);
+
 template <typename T>
 static void fill_info(const Plan<T>* p, cufinufft_plan_info* info) {
   std::memset(info, 0, sizeof(*info));

@@ -1,7 +1,10 @@
 // batch.cu -- the batch C ABI: building the descriptor tables, capturing the
 // batch sequence into a CUDA graph and replaying it (kernels in batch.cuh,
 // instantiated per precision in batch_f.cu / batch_d.cu).
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 
 #include "batch.cuh"
 
@@ -119,6 +122,48 @@ static int batch_record(Batch<T>* b) {
   return 0;
 }
 
+// The batch as every plan's own execute: plans go, heaviest first, to the
+// least-loaded of the kSide branch streams (load = taps + grid cells), each
+// running its own tuned spread/interp kernels, cuFFT plans and
+// deconvolution there.
+template <typename T>
+static int batch_record_plans(Batch<T>* b, cplx_t<T>** c, cplx_t<T>** fk) {
+  const int n = (int)b->plans.size();
+  constexpr int K = Batch<T>::kSide;
+  b->evnext = 0;
+  std::vector<double> w(n);
+  std::vector<int> order(n), branch(n);
+  for (int i = 0; i < n; ++i) {
+    const Plan<T>* p = b->plans[i];
+    w[i] = (double)p->M * p->ntransf * std::pow((double)p->sp.ns, p->dim) +
+           8.0 * (double)grid_cells(p) * p->ntransf + 1.0;
+    order[i] = i;
+  }
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return w[x] > w[y]; });
+  double load[K] = {};
+  for (int i : order) {
+    int k = 0;
+    for (int q = 1; q < K; ++q)
+      if (load[q] < load[k]) k = q;
+    branch[i] = k;
+    load[k] += w[i];
+  }
+  for (int k = 0; k < K; ++k)
+    if (load[k] > 0) CFG_CUDA(follow(b, b->stream, b->side[k]));
+  for (int i : order) {
+    Plan<T>* p = b->plans[i];
+    cudaStream_t own = p->stream;
+    int e = plan_use_stream(p, b->side[branch[i]]);
+    if (!e) e = execute_plan(p, c[i], fk[i]);
+    const int e2 = plan_use_stream(p, own);
+    if (e) return e;
+    if (e2) return e2;
+  }
+  for (int k = 0; k < K; ++k)
+    if (load[k] > 0) CFG_CUDA(follow(b, b->side[k], b->stream));
+  return 0;
+}
+
 // Type-1 groups: consecutive plans cut where the running tap count (M ntr
 // ns^d per plan) crosses k / kBatchGroups of the total, so each group's spread
 // is about as long and its FFTs overlap the next group's spreading.
@@ -187,6 +232,11 @@ static int batch_make(Batch<T>* b, int nplans, Plan<T>** plans) {
   CFG_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
   for (int k = 0; k < Batch<T>::kSide; ++k)
     CFG_CUDA(cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
+  // default: the graph of each plan's own execute; CUFINUFFT_BATCH=tables
+  // selects the multi-plan kernels over descriptor tables
+  const char* mode = std::getenv("CUFINUFFT_BATCH");
+  b->by_plans = !(mode && std::strcmp(mode, "tables") == 0);
+  if (b->by_plans) return 0;
   CFG_CUDA(cudaMallocHost(&b->h_desc, sizeof(BatchDesc<T>) * nplans));
   CFG_CUDA(cudaMalloc(&b->d_desc, sizeof(BatchDesc<T>) * nplans));
   long long task = 0, row = 0, blk = 0;
@@ -273,6 +323,7 @@ static int batch_execute(Batch<T>* b, cplx_t<T>** c, cplx_t<T>** fk) {
   if (b->launched) CFG_CUDA(cudaEventSynchronize(b->done));
   for (int i = 0; i < n; ++i) {
     if ((b->plans[i]->M > 0 && c[i] == nullptr) || fk[i] == nullptr) return CUFINUFFT_ERR_ARG;
+    if (b->by_plans) continue;
     BatchDesc<T>& D = b->h_desc[i];
     if (b->type == 1) {
       D.c_in = c[i];
@@ -286,11 +337,23 @@ static int batch_execute(Batch<T>* b, cplx_t<T>** c, cplx_t<T>** fk) {
   // order after the legacy default stream, as a plan's stream is
   CFG_CUDA(cudaEventRecord(b->done, cudaStreamLegacy));
   CFG_CUDA(cudaStreamWaitEvent(b->stream, b->done, 0));
+  if (b->by_plans && b->gexec != nullptr &&
+      !(std::equal(b->cap_c.begin(), b->cap_c.end(), c) && std::equal(b->cap_fk.begin(), b->cap_fk.end(), fk))) {
+    // other caller arrays: capture again
+    cudaGraphExecDestroy(b->gexec);
+    cudaGraphDestroy(b->graph);
+    b->gexec = nullptr;
+    b->graph = nullptr;
+  }
   if (b->gexec == nullptr) {
     cudaStreamCaptureStatus st;
     bool captured = false;
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      int e = batch_record(b);
+      int e = b->by_plans ? batch_record_plans(b, c, fk) : batch_record(b);
+      if (b->by_plans) {
+        b->cap_c.assign(c, c + n);
+        b->cap_fk.assign(fk, fk + n);
+      }
       cudaGraph_t g = nullptr;
       cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
       if (e == 0 && ce == cudaSuccess && g != nullptr &&
@@ -305,7 +368,7 @@ static int batch_execute(Batch<T>* b, cplx_t<T>** c, cplx_t<T>** fk) {
     cudaGetLastError();
     if (!captured) {
       b->gexec = nullptr;
-      int e = batch_record(b);  // direct launches
+      int e = b->by_plans ? batch_record_plans(b, c, fk) : batch_record(b);  // direct launches
       if (e) return e;
       CFG_CUDA(cudaEventRecord(b->done, b->stream));
       b->launched = true;

@@ -453,6 +453,11 @@ template <typename T> struct Batch {
   std::vector<cudaEvent_t> evpool;  // events of the recorded sequence
   size_t evnext = 0;
   unsigned fft_used = 0;            // FFT streams the recorded sequence used (bit k: side[2 + k])
+  // by_plans: the graph holds every plan's own execute (its tuned kernels) on
+  // parallel branches instead of multi-plan kernels; it bakes in the
+  // caller's arrays, so it is captured again when they change
+  bool by_plans = false;
+  std::vector<const void*> cap_c, cap_fk;
   int type = 0, dim = 0, ns = 0, device = 0;
   std::vector<cplx_t<T>*> fw;
   std::vector<cufftHandle> fft;

@@ -187,6 +187,13 @@ inline SpreadArgs<T> spread_args(Plan<T>* p) {
   return a;
 }
 
+// A plan's whole execute, and moving its work (cuFFT plans included) to
+// another stream (api.cu; used by the batch).
+template <typename T>
+int execute_plan(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk);
+template <typename T>
+int plan_use_stream(Plan<T>* p, cudaStream_t s);
+
 template <typename T>
 inline cudaError_t run_spread(Plan<T>* p, const SpreadArgs<T>& a) {
   switch (p->dim) {

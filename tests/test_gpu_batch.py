@@ -51,13 +51,18 @@ def _run_single(plan, ntype, modes, M, ntr, data):
     return out.cpu().numpy()
 
 
+@pytest.mark.parametrize("mode", ["tables", "plans"])
 @pytest.mark.parametrize("single", [True, False], ids=["f32", "f64"])
 @pytest.mark.parametrize("ntype", [1, 2])
 @pytest.mark.parametrize("dim", [2, 3])
-def test_batch_matches_each_plan(single, ntype, dim):
+def test_batch_matches_each_plan(monkeypatch, mode, single, ntype, dim):
+    """Both batch forms: multi-plan kernels over descriptor tables, and a
+    graph of every plan's own execute (captured again when the arrays
+    change, as they do on every repetition here)."""
     import torch
 
     from cufinufft_gb300 import cufinufft_batch
+    monkeypatch.setenv("CUFINUFFT_BATCH", mode)
     plans, inputs = _plans(ntype, single, dim, seed=100 * dim + ntype)
     refs = [_run_single(p, ntype, *inp[:3], inp[4]) for p, inp in zip(plans, inputs)]
     batch = cufinufft_batch(plans)
