@@ -191,10 +191,12 @@ int cufinufft_mlp_adam(float* params, const float* grad, float* m, float* v, int
  * executed together.  batch_make takes plans whose points are set (they must
  * outlive the batch and keep their points); batch_execute takes host arrays
  * of nplans device pointers (c[i], fk[i] as for plan i's execute) and runs
- * every plan's whole ntransf at once: multi-plan spread/interp and
- * deconvolve/amplify kernels plus one cuFFT call per plan, captured once as a
- * CUDA graph and replayed.  Results are ordered before later work on the
- * legacy default stream. */
+ * every plan's whole ntransf at once: one CUDA-graph replay of every plan's
+ * own execute on parallel branches (captured again when the arrays change;
+ * with CUFINUFFT_BATCH=tables, multi-plan spread/interp and
+ * deconvolve/amplify kernels over a descriptor table plus one cuFFT call per
+ * plan).  A plan must not run on its own while its batch runs.  Results are
+ * ordered before later work on the legacy default stream. */
 typedef struct cufinufft_batch_s* cufinufft_batch;
 typedef struct cufinufftf_batch_s* cufinufftf_batch;
 int cufinufft_batch_make(int nplans, cufinufft_plan* plans, cufinufft_batch* batch);
