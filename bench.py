@@ -300,7 +300,17 @@ def accuracy(w: Workload, out_first: np.ndarray, seed=3):
         idx = rng.choice(M, size=min(M, w.acc_n), replace=False)
         ref = O.direct_type2(*pts, data.ravel(), w.modes, -1, idx)
     est = out_first.ravel()[idx].astype(np.complex128)
-    return float(np.linalg.norm(est - ref) / np.linalg.norm(ref)), int(idx.size)
+    err = float(np.linalg.norm(est - ref) / np.linalg.norm(ref))
+    # the same transform by the oracle (FP64 arithmetic, the reference's kernel
+    # width and shape for this tol) at the same modes/targets: the error the
+    # reference's parameter rule itself leaves, beside ours
+    oracle_err = None
+    if pts[0].size <= 4_000_000:
+        plan = oracle_plan(w, os.cpu_count() or 1)
+        full = cpu_step(plan, w, [p for p in pts if p is not None], w.data().astype(np.complex128))
+        o = np.asarray(full)[0].ravel()[idx]
+        oracle_err = float(np.linalg.norm(o - ref) / np.linalg.norm(ref))
+    return err, int(idx.size), oracle_err
 
 
 # --------------------------------------------------------------------------
@@ -523,7 +533,7 @@ def run_ours(args, w: Workload, rank, world, local_rank):
     units = M * w.ntransf
     value = world * units * args.steps / (dev_ms / 1e3)
     e2e_value = world * units * args.steps / (e2e_ms / 1e3)
-    err, nacc = accuracy(w, out_first) if not args.no_accuracy else (None, 0)
+    err, nacc, oracle_err = accuracy(w, out_first) if not args.no_accuracy else (None, 0, None)
 
     # roofline of the dominant kernel of ours: spread (type 1) / interp (type 2)
     s = 4 if w.single else 8
@@ -564,6 +574,7 @@ def run_ours(args, w: Workload, rank, world, local_rank):
                    "method": info["method"], "ns": info["ns"], "nf": nf[:w.dim],
                    "kerevalmeth": info["kerevalmeth"]},
         "rel_l2_err": err, "rel_l2_points": nacc, "tol": w.tol,
+        "rel_l2_err_oracle_same_width": oracle_err,
         "plain": None if plain_ms is None else {
             "value": units / (plain_ms / 1e3), "ms_per_step": plain_ms,
             "method": plain_info["method"],
