@@ -414,11 +414,36 @@ def run_ours(args, w: Workload, rank, world, local_rank):
     inp, out, args_ce = _io_tensors(w, data_dev, M, dev)
     with torch.cuda.stream(stream):
         plan.set_pts(*pts_dev[::-1])  # the Python interface takes C-ordered axes
+    torch.cuda.synchronize()
+    selector_info = plan.info()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    tune = None
+    if args.method == 0:
+        # tuned form: the learned selector's layout (gpu_method 0) against the
+        # library autotuner's best layout class on a second plan over the same
+        # points; a few flushed executes of each decide which is timed
+        alt = _make_plan(w, dev, stream, opts)
+        with torch.cuda.stream(stream):
+            alt.set_pts(*pts_dev[::-1])
+        torch.cuda.synchronize()
+        best = alt.autotune()[0]
+        if (best["method"], best["binsizex"], best["binsizey"], best["binsizez"]) != (
+                selector_info["method"], selector_info["binsizex"], selector_info["binsizey"],
+                selector_info["binsizez"]):
+            k = 3
+            for p in (plan, alt):
+                _time_device(p, args_ce, 1, stream, flush)
+            t_sel = _time_device(plan, args_ce, k, stream, flush)
+            t_alt = _time_device(alt, args_ce, k, stream, flush)
+            if t_alt < t_sel:
+                plan, alt = alt, plan
+                tune = best
+        del alt
+    with torch.cuda.stream(stream):
         plan.execute(*args_ce)
     torch.cuda.synchronize()
     info = plan.info()
     out_first = out.cpu().numpy()
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def barrier():
         if dist is not None:
@@ -468,6 +493,9 @@ def run_ours(args, w: Workload, rank, world, local_rank):
     plans = [plan, _make_plan(w, dev, streams[1], opts)]
     with torch.cuda.stream(streams[1]):
         plans[1].set_pts(*pts_dev[::-1])
+    if tune is not None:
+        plans[1].set_layout(tune["method"], (tune["binsizex"], tune["binsizey"], tune["binsizez"]),
+                            tune["maxsubprobsize"])
     stage_in = [torch.empty_like(inp) for _ in range(2)]
     stage_out = [torch.empty_like(out) for _ in range(2)]
 
@@ -569,10 +597,19 @@ def run_ours(args, w: Workload, rank, world, local_rank):
         "config": {"workload": w.desc, "name": w.name, "global_batch": world, "seq_len": None,
                    "parallelism": f"replicas x{world}",
                    "l2": "flushed between steps (256 MB write, outside the timed events)",
-                   "form": "tuned (gpu_method chosen by the library)" if args.method == 0
+                   "form": "tuned (gpu_method 0: the learned selector's layout, or the library "
+                           "autotuner's best of its twelve layout classes when that executes "
+                           "faster on this plan's points)" if args.method == 0
                    else f"gpu_method {args.method}",
                    "method": info["method"], "ns": info["ns"], "nf": nf[:w.dim],
-                   "kerevalmeth": info["kerevalmeth"]},
+                   "bins": [info["binsizex"], info["binsizey"], info["binsizez"]][:w.dim],
+                   "kerevalmeth": info["kerevalmeth"],
+                   "layout_from": None if args.method != 0 else (
+                       "autotuner" if tune is not None else "selector"),
+                   "selector_pick": None if args.method != 0 else {
+                       "method": selector_info["method"],
+                       "bins": [selector_info["binsizex"], selector_info["binsizey"],
+                                selector_info["binsizez"]][:w.dim]}},
         "rel_l2_err": err, "rel_l2_points": nacc, "tol": w.tol,
         "rel_l2_err_oracle_same_width": oracle_err,
         "plain": None if plain_ms is None else {
@@ -778,8 +815,8 @@ def run_batch64(args, rank, world, local_rank):
         "config": {"workload": wl.desc, "name": wl.name, "plans": len(specs),
                    "nu_point_transforms": units,
                    "l2": "flushed between steps (256 MB write, outside the timed events)",
-                   "form": "tuned+batched: gpu_method 0, one CUDA-graph replay of multi-plan "
-                           "kernels"},
+                   "form": "tuned+batched: every plan autotuned, one CUDA-graph replay of "
+                           "all plans' executes on parallel branches"},
         "plain": {"value": units / (plain_ms / 1e3), "ms_per_step": plain_ms,
                   "note": "the 64 plans with the reference's default options, executed one "
                           "after another on one stream"},
