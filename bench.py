@@ -686,11 +686,13 @@ def run_batch64(args, rank, world, local_rank):
     stream = torch.cuda.Stream(device=dev)
     units = sum(s["M"] * s["ntr"] for s in specs)
 
-    def build(opts):
+    def build(opts, whole_batch=False):
+        # whole_batch: all of a plan's transforms in one pass (maxbatchsize =
+        # ntransf) instead of the reference's default min(ntransf, 8)
         plans, cs, fks, pts_keep = [], [], [], []
         for s in specs:
             p = cufinufft(1, s["modes"][::-1], n_trans=s["ntr"], eps=wl.tol, dtype=np.float32,
-                          maxbatchsize=0, **opts)
+                          maxbatchsize=s["ntr"] if whole_batch else 0, **opts)
             p.set_stream(stream)
             pd = [torch.from_numpy(x).to(dev) for x in s["pts"]]
             with torch.cuda.stream(stream):
@@ -734,7 +736,7 @@ def run_batch64(args, rank, world, local_rank):
 
     # batched with the library's default choice (gpu_method 0), one graph
     # replay of multi-plan kernels
-    tuned, cs2, fks2, keep2 = build({"gpu_method": 0})
+    tuned, cs2, fks2, keep2 = build({"gpu_method": 0}, whole_batch=True)
     batch = cufinufft_batch(tuned)
 
     def run_batch_default():
