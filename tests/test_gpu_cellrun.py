@@ -93,7 +93,7 @@ def test_reference_method3_is_cell_run():
                           1e-5, True)
     err = np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
     err2 = np.linalg.norm(plain.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
-    # FP32 sums of thousands of terms per cell: judged against the plain
+    # FP32 sums of thousands of terms per cell: compared against the plain
     # method-2 spread's own FP32 error on the same input
     assert err < max(2e-5, 1.5 * err2), (err, err2)
 
