@@ -31,10 +31,13 @@
 namespace cfg {
 
 constexpr int kSpreadThreads = 256;
-// Threads of a k_interp_sm block, and its blocks per SM at the FP32
-// register bound (40 registers a thread for ns <= 9).
+// Threads of a k_interp_sm block, and the blocks per SM its register bound
+// is set for: FP32 6 (40 registers a thread for ns <= 9; 4 above), FP64 2
+// (128 registers: radial 2D FP64 at ns 13 interpolates 4% faster than at one
+// block of 188 registers, despite 52 bytes of spill).
 constexpr int kInterpThreads = 256;
 constexpr int kInterpBlocksF32 = 6 * 256 / kInterpThreads;
+constexpr int kInterpBlocksF64 = 2 * 256 / kInterpThreads;
 
 // Subproblem header shared by the shared-memory kernels.
 struct SubTile {
@@ -538,7 +541,7 @@ struct InterpPoint {
 // wait: evaluated before it, the rows stay live across the wait and the FP32
 // kernels spill at the 40-register bound (measured 3.5% slower).
 template <typename T, int DIM, int NS>
-__global__ void __launch_bounds__(kInterpThreads, sizeof(T) == 4 ? (NS <= 9 ? kInterpBlocksF32 : kInterpBlocksF32 * 2 / 3) : 1)
+__global__ void __launch_bounds__(kInterpThreads, sizeof(T) == 4 ? (NS <= 9 ? kInterpBlocksF32 : kInterpBlocksF32 * 2 / 3) : kInterpBlocksF64)
 k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) {
   using C = cplx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
