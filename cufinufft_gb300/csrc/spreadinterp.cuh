@@ -17,7 +17,9 @@
 //   * FP32 plans evaluate the kernel in FP32 (the reference promotes the
 //     FP32 build's kernel to FP64, src/cuspreadinterp.h:15);
 //   * the tile is bs + ns - 1 wide (the reference pads 2*ceil(ns/2)), and the
-//     flush skips cells no point touched.
+//     flush skips cells no point touched;
+//   * interpolation tiles that do not wrap the periodic edge arrive by one
+//     tiled bulk copy (TMA, cp.async.bulk.tensor) instead of per-cell loads.
 #pragma once
 
 #include <cuda.h>  // CUtensorMap and its encoder's types (the encoder is fetched at run time)
