@@ -314,6 +314,24 @@ def accuracy(w: Workload, out_first: np.ndarray, seed=3):
 
 
 # --------------------------------------------------------------------------
+# Replicas: every rank runs the whole workload on its own GPU; nothing moves
+# between ranks except the timings.
+def reduce_max(vals, dist, device):
+    """Max over the ranks of each value in `vals` (floats); no-op on one rank."""
+    import torch
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=device)
+    if dist is not None and dist.is_initialized():
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def replica_rate(world, units, steps, ms):
+    """Whole-job rate: `world` replicas each did `units` per step for `steps`
+    steps, and the slowest took `ms` in total."""
+    return world * units * steps / (ms / 1e3)
+
+
+# --------------------------------------------------------------------------
 def run_reference(args, w: Workload, rank, world):
     if rank != 0:
         return
@@ -556,16 +574,13 @@ def run_ours(args, w: Workload, rank, world, local_rank):
         if not np.allclose(out_host[k].numpy(), out_first, rtol=0, atol=1e-4 * scale):
             raise RuntimeError("e2e output differs from the device-resident run")
 
-    times = torch.tensor([dev_ms, e2e_ms, e2e_pipe_ms], dtype=torch.float64, device=dev)
-    if dist is not None:
-        dist.all_reduce(times, op=dist.ReduceOp.MAX)
-    dev_ms, e2e_ms, e2e_pipe_ms = float(times[0]), float(times[1]), float(times[2])
+    dev_ms, e2e_ms, e2e_pipe_ms = reduce_max([dev_ms, e2e_ms, e2e_pipe_ms], dist, dev)
     if rank != 0:
         return
 
     units = M * w.ntransf
-    value = world * units * args.steps / (dev_ms / 1e3)
-    e2e_value = world * units * args.steps / (e2e_ms / 1e3)
+    value = replica_rate(world, units, args.steps, dev_ms)
+    e2e_value = replica_rate(world, units, args.steps, e2e_ms)
     err, nacc, oracle_err = accuracy(w, out_first) if not args.no_accuracy else (None, 0, None)
 
     # roofline of the dominant kernel of ours: spread (type 1) / interp (type 2)
@@ -627,7 +642,7 @@ def run_ours(args, w: Workload, rank, world, local_rank):
                 "note": "public Python/C-ABI execute with the input copied from pinned host "
                         "memory and the output copied back inside each step's events; L2 "
                         "flushed between steps",
-                "pipelined": {"value": world * units * args.steps / (e2e_pipe_ms / 1e3),
+                "pipelined": {"value": replica_rate(world, units, args.steps, e2e_pipe_ms),
                               "ms_per_step": e2e_pipe_ms / args.steps,
                               "note": "same calls as a continuous stream: two plans on two "
                                       "streams alternate so one step's copies overlap the "
