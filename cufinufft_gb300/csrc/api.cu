@@ -88,7 +88,15 @@ template <typename T> static void free_points(Plan<T>* p) {
   p->capM = 0;
 }
 
+template <typename T> static void drop_graph(Plan<T>* p) {
+  if (p->gexec) cudaGraphExecDestroy(p->gexec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->gexec = nullptr;
+  p->graph = nullptr;
+}
+
 template <typename T> static void release(Plan<T>* p) {
+  drop_graph(p);
   if (p->have_fft) cufftDestroy(p->fft);
   if (p->have_fft_rem) cufftDestroy(p->fft_rem);
   p->have_fft = p->have_fft_rem = false;
@@ -686,6 +694,7 @@ static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
   for (int k = 0; k < p->dim; ++k)
     if (M > 0 && xs[k] == nullptr) return CUFINUFFT_ERR_ARG;
   p->pts_set = false;
+  ++p->version;  // point arrays may be reallocated below
   int e = ensure_points(p, M);
   if (e) return e;
   p->M = M;
@@ -781,7 +790,7 @@ static int collect_times(Plan<T>* p) {
 }
 
 template <typename T>
-static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
+static int execute_direct(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
   if (!p->planned) return CUFINUFFT_ERR_GENERIC;
   if (p->type != 1 && p->type != 2) return CUFINUFFT_ERR_GENERIC;
   if (p->method == 0) return CUFINUFFT_ERR_METHOD;
@@ -863,11 +872,58 @@ static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
   return 0;
 }
 
+// CUFINUFFT_GRAPH=0: every execute launches its kernels directly.
+static bool graphs_enabled() {
+  const char* v = std::getenv("CUFINUFFT_GRAPH");
+  return !(v && v[0] == '0');
+}
+
+// execute: with stage timing off, the launch sequence is captured once as a
+// CUDA graph (for these caller arrays and this plan state) and replayed, which
+// removes most of the gaps between its kernels.  A plan stream that is already
+// being captured (a batch recording this plan), or a capture that fails, runs
+// the kernels directly.
+template <typename T>
+static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
+  if (p->timing || !p->planned || !graphs_enabled()) return execute_direct(p, c, fk);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    cudaGetLastError();
+    return execute_direct(p, c, fk);
+  }
+  if (p->gexec && p->g_c == c && p->g_fk == fk && p->g_version == p->version) {
+    CFG_CUDA(cudaGraphLaunch(p->gexec, p->stream));
+    return 0;
+  }
+  drop_graph(p);
+  if (cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    const int e = execute_direct(p, c, fk);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(p->stream, &g);
+    if (e == 0 && ce == cudaSuccess && g != nullptr &&
+        cudaGraphInstantiate(&p->gexec, g, 0) == cudaSuccess) {
+      p->graph = g;
+      p->g_c = c;
+      p->g_fk = fk;
+      p->g_version = p->version;
+      CFG_CUDA(cudaGraphLaunch(p->gexec, p->stream));
+      return 0;
+    }
+    if (g) cudaGraphDestroy(g);
+    p->gexec = nullptr;
+    cudaGetLastError();  // a failed capture leaves its error behind
+    if (e) return e;     // the plan or the arguments are at fault, not the capture
+  } else {
+    cudaGetLastError();
+  }
+  return execute_direct(p, c, fk);
+}
+
 // Entry points for the batch (batch.cu): a plan's whole execute, and moving
 // a plan's work, cuFFT plans included, to another stream.
 template <typename T>
 int execute_plan(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
-  return execute_impl(p, c, fk);
+  return execute_direct(p, c, fk);
 }
 template <typename T>
 int plan_use_stream(Plan<T>* p, cudaStream_t s) {
@@ -989,6 +1045,7 @@ static int build_subproblems(Plan<T>* p) {
 template <typename T>
 static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub) {
   if (!p->planned) return CUFINUFFT_ERR_GENERIC;
+  ++p->version;  // the sorted arrays and bin tables are about to move
   // method 5: method 2 spreading over cell-ordered points (cell-run kernel)
   const bool cell = method == 5;
   if (cell) {

@@ -73,6 +73,13 @@ template <typename T> struct Plan {
   unsigned char* sub_dense = nullptr;  // per subproblem: starts on a dense cell (cell order)
   size_t cap_sub_dense = 0;
   int* h_total = nullptr;  // pinned readback of the subproblem count
+  // execute as a CUDA graph (timing off): captured for one pair of caller
+  // arrays and one plan state (`version` counts setpts / set_layout)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  const void* g_c = nullptr;
+  const void* g_fk = nullptr;
+  unsigned version = 0, g_version = 0;
   // stage timing (extension): events recorded around each stage of execute
   bool timing = false;
   std::vector<cudaEvent_t> ev_pool;   // free events
