@@ -752,9 +752,22 @@ def run_batch64(args, rank, world, local_rank):
             for p, c, f in zip(plain, cs, fks):
                 p.execute(c, f)
 
+    # twice: kernels launched directly, as the reference launches them
+    # (CUFINUFFT_GRAPH=0), and with each execute replaying its plan's graph
+    saved_env = os.environ.get("CUFINUFFT_GRAPH")
+    os.environ["CUFINUFFT_GRAPH"] = "0"
+    try:
+        for _ in range(args.warmup):
+            run_plain()
+        plain_ms = timed(run_plain, args.steps)
+    finally:
+        if saved_env is None:
+            os.environ.pop("CUFINUFFT_GRAPH", None)
+        else:
+            os.environ["CUFINUFFT_GRAPH"] = saved_env
     for _ in range(args.warmup):
         run_plain()
-    plain_ms = timed(run_plain, args.steps)
+    plain_graph_ms = timed(run_plain, args.steps)
     out_plain = [f.cpu().numpy() for f in fks[:8]]
     del plain
 
@@ -850,8 +863,11 @@ def run_batch64(args, rank, world, local_rank):
                            "all plans' executes on parallel branches"},
         "plain": {"value": units / (plain_ms / 1e3), "ms_per_step": plain_ms,
                   "note": "the 64 plans with the reference's default options, executed one "
-                          "after another on one stream"},
+                          "after another on one stream, kernels launched directly as the "
+                          "reference launches them (CUFINUFFT_GRAPH=0)",
+                  "graph_replay_ms_per_step": plain_graph_ms},
         "speedup_vs_plain": plain_ms / batch_ms,
+        "speedup_vs_plain_graph_replay": plain_graph_ms / batch_ms,
         "batched_default_ms": default_ms, "batched_tuned_warmup_ms": tuned_warm_ms,
         "autotune": {"seconds": tune_s, "policy": policy,
                      "per_plan_choice": {f"method {m} bins {b}" + (f" maxsub {c}" if c else ""): n
