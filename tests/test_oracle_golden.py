@@ -130,3 +130,54 @@ def test_oracle_pipeline_meets_tol(dim, modes, ntype, single, tol):
         ref = O.direct_type2(*pts, fk, modes, -1, np.arange(M))
         err = O.rel_l2(c, ref)
     assert err < 5 * tol, err
+
+
+def _np_spread(dim, nf, pts, c, ns, beta, es_c):
+    """Plain numpy restatement of the spreader (RESCALE fold,
+    contrib/spreadinterp.h:36-38; taps ceil(xr - ns/2) .. + ns - 1 with
+    phi = exp(beta sqrt(1 - c x^2)) inside the support,
+    src/cuspreadinterp.h:6-40; periodic wrap) for small grids."""
+    grid = np.zeros(tuple(nf[::-1]), dtype=np.complex128)
+    for p in range(c.size):
+        taps = []
+        for d in range(dim):
+            x = pts[d][p]
+            sh = 1.5 if x < -np.pi else (-0.5 if x >= np.pi else 0.5)
+            xr = (x / (2 * np.pi) + sh) * nf[d]
+            j0 = int(np.ceil(xr - ns / 2.0))
+            idx = [(j0 + j) % nf[d] for j in range(ns)]
+            ker = []
+            for j in range(ns):
+                z = (j0 + j) - xr
+                ker.append(0.0 if abs(z) >= ns / 2.0 else np.exp(beta * np.sqrt(1.0 - es_c * z * z)))
+            taps.append((idx, ker))
+        if dim == 1:
+            for (i, k) in zip(*taps[0]):
+                grid[i] += c[p] * k
+        else:
+            for (iy, ky) in zip(*taps[1]):
+                for (ix, kx) in zip(*taps[0]):
+                    grid[iy, ix] += c[p] * kx * ky
+    return grid
+
+
+@pytest.mark.parametrize("grid", [(40,), (24, 20)])
+def test_oracle_spread_on_a_given_grid_matches_numpy(grid):
+    """The oracle's spread with the grid given directly (spread/interp-only
+    plans): against a numpy restatement, FP64 parameters at tol 1e-8."""
+    rng = np.random.default_rng(17)
+    dim, M = len(grid), 60
+    pts = [rng.uniform(-np.pi, np.pi, M) for _ in range(dim)]
+    c = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    plan = O.OraclePlan(1, grid, 1, 1e-8, False, spreadinterponly=True)
+    assert plan.nf == tuple(grid)
+    args = pts + [None] * (3 - dim)
+    got = plan.spread(*args, c=c, ntr=1)[0].reshape(tuple(grid[::-1]))
+    ref = _np_spread(dim, grid, pts, c, plan.ns, plan.beta, plan.c)
+    assert np.allclose(got, ref, rtol=1e-12, atol=1e-9 * np.abs(ref).max())
+    # interpolation is the adjoint: <spread(c), g> = <c, interp(g)>
+    g = rng.standard_normal(tuple(grid[::-1])) + 1j * rng.standard_normal(tuple(grid[::-1]))
+    back = plan.interp(*args, fw=g, ntr=1)[0]
+    lhs = np.vdot(g.ravel(), got.ravel())
+    rhs = np.vdot(back, c)
+    assert abs(lhs - rhs) <= 1e-9 * abs(lhs)
