@@ -79,7 +79,10 @@ int cufinufftf_setpts(int M, float* x, float* y, float* z, int N, float* s,
 
 /* Run ntransf transforms: type 1 reads c (ntransf*M) and writes fk
  * (ntransf*N1*N2*N3); type 2 reads fk and writes c.  Replaces
- * CUFINUFFT_EXECUTE, src/cufinufft.cu:495-569. */
+ * CUFINUFFT_EXECUTE, src/cufinufft.cu:495-569.  With stage timing off the
+ * launch sequence is captured as a CUDA graph the first time a pair (c, fk)
+ * is seen and replayed after that; setpts / set_layout, or other arrays,
+ * capture it again (CUFINUFFT_GRAPH=0: direct launches every time). */
 int cufinufft_execute(cuDoubleComplex* c, cuDoubleComplex* fk,
                       cufinufft_plan plan);
 int cufinufftf_execute(cuFloatComplex* c, cuFloatComplex* fk,
