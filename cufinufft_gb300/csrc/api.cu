@@ -506,6 +506,7 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
 
   p->iflag = iflag >= 0 ? 1 : -1;
   p->ntransf = ntransf;
+  if (type == 2) tma_encoder();  // first lookup outside any capture of execute
   if (maxbatchsize == 0) maxbatchsize = std::min(ntransf, 8);
   p->maxbatch = std::min(maxbatchsize, ntransf);
   p->rem = ntransf % p->maxbatch;
@@ -870,6 +871,21 @@ static int execute_direct(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
     mark(p, ev[3]);
   }
   return 0;
+}
+
+void* tma_encoder() {
+  static void* const fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();  // no encoder: interpolation tiles stay on the per-cell path
+      f = nullptr;
+    }
+    return f;
+  }();
+  return fn;
 }
 
 // CUFINUFFT_GRAPH=0: every execute launches its kernels directly.

@@ -107,6 +107,11 @@ struct SubClassArgs {
   unsigned char* dense;
 };
 cudaError_t launch_classify_subproblems(const SubClassArgs& a, cudaStream_t s);
+// The driver's cuTensorMapEncodeTiled, looked up once per process (null if
+// the driver has none).  makeplan looks it up for type-2 plans, so the first
+// lookup does not happen inside a stream capture.
+void* tma_encoder();
+
 cudaError_t launch_sub_to_bin(const int* sub_start, int nbins, int nsub, int* sub_to_bin,
                               cudaStream_t s);
 // sub_to_bin plus the subproblem headers (hdr[nsub]) of bins bs x nb holding

@@ -259,15 +259,7 @@ bool grid_tensor_map(CUtensorMap* map, const cplx_t<T>* grid, const GridGeom& g,
   using Encode = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                               const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-  static const Encode encode = [] {
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
-            cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      fn = nullptr;
-    return reinterpret_cast<Encode>(fn);
-  }();
+  const Encode encode = reinterpret_cast<Encode>(tma_encoder());
   if (const char* v = std::getenv("CUFINUFFT_TMA"))
     if (v[0] == '0') return false;
   if (!encode || grid == nullptr || ntr < 1) return false;
