@@ -25,9 +25,16 @@ def _rank(rank, world, port, out):
         dist.destroy_process_group()
 
 
+def _free_port():
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
 def test_max_over_two_gloo_ranks():
     world = 2
-    port = 29500 + (os.getpid() % 1000)
+    port = _free_port()
     with mp.Manager() as m:
         out = m.dict()
         mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
