@@ -100,3 +100,30 @@ def test_python_wrapper_rejects_unknown_option(lib):
     assert "Invalid option 'foo'" in err.value.args[0]
     with pytest.raises(TypeError):
         cufinufft(1, (8, 8), dtype=np.int32)
+
+
+def _struct_fields(header, name):
+    """Field names and C types of `typedef struct name { ... } name;` in order."""
+    txt = open(os.path.join(ROOT, "include", header)).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    body = re.search(r"typedef struct " + name + r"\s*\{(.*?)\}\s*" + name + ";", txt, flags=re.S).group(1)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        ctype, names = decl.split(None, 1)
+        fields += [(n.strip(), ctype) for n in names.split(",")]
+    return fields
+
+
+def test_plan_info_mirror_matches_header():
+    """The Python mirror of cufinufft_plan_info (an extension struct) has the
+    header's fields in the header's order, with the same C types."""
+    from cufinufft_gb300._cufinufft import PlanInfo
+    want = _struct_fields("cufinufft.h", "cufinufft_plan_info")
+    ct = {"int": ctypes.c_int, "double": ctypes.c_double}
+    got = [(f, t) for f, t in PlanInfo._fields_]
+    assert [f for f, _ in got] == [f for f, _ in want]
+    for (f, t), (_, c) in zip(got, want):
+        assert t == ct[c], f
