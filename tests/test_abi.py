@@ -127,3 +127,17 @@ def test_plan_info_mirror_matches_header():
     assert [f for f, _ in got] == [f for f, _ in want]
     for (f, t), (_, c) in zip(got, want):
         assert t == ct[c], f
+
+
+@pytest.mark.parametrize("header,name,mirror", [
+    ("cufinufft.h", "cufinufft_tune_entry", "TuneEntry"),
+    ("cufinufft_opts.h", "cufinufft_opts", "NufftOpts"),
+])
+def test_other_struct_mirrors_match_headers(header, name, mirror):
+    from cufinufft_gb300 import _cufinufft
+    want = _struct_fields(header, name)
+    ct = {"int": ctypes.c_int, "double": ctypes.c_double, "float": ctypes.c_float}
+    got = getattr(_cufinufft, mirror)._fields_
+    assert [f for f, _ in got] == [f for f, _ in want]
+    for (f, t), (_, c) in zip(got, want):
+        assert t == ct[c], f
