@@ -233,7 +233,11 @@ static inline int orc_taps(double xr, int ns, double beta, double c,
 /* Coloured bin schedule for a race-free parallel spread: bins of width bs
  * (bs >= ns) in each dimension; a point belongs to the bin of its first tap.
  * Colour per dimension: b%2, and colour 2 for the last bin when nbins is odd,
- * so bins that share a colour never touch the same fine-grid cell.  This is
+ * so bins that share a colour never touch the same fine-grid cell.  A bin
+ * writes its own cells and the ns-1 cells after them (periodically), so a
+ * last bin narrower than ns-1 cells would let the halo of the bin before it
+ * wrap into bin 0; such a sliver is merged into the bin before it (the last
+ * bin is then between bs and 2 bs - 1 cells wide).  This is
  * the CPU form of the subproblem method (src/2d/spreadinterp2d.cu:152-231):
  * points are grouped by bin and each group is added to the grid by one
  * thread. */
@@ -258,6 +262,7 @@ void orc_spread(int dim, int nf1, int nf2, int nf3, int M, const double* x,
     bs[d] = d < dim ? (bdef < ns ? ns : bdef) : 1;
     if (d < dim && bs[d] > nf[d]) bs[d] = nf[d];
     nb[d] = (nf[d] + bs[d] - 1) / bs[d];
+    if (nb[d] > 1 && nf[d] - (nb[d] - 1) * bs[d] < ns - 1) nb[d] -= 1;
   }
   long long nbins = (long long)nb[0] * nb[1] * nb[2];
   /* bin every point by its first tap */
@@ -270,7 +275,7 @@ void orc_spread(int dim, int nf1, int nf2, int nf3, int M, const double* x,
       double xr = orc_rescale(co[d][j], nf[d]);
       int s = (int)ceil(xr - ns / 2.0);
       s = ((s % nf[d]) + nf[d]) % nf[d];
-      bidx[d] = s / bs[d];
+      bidx[d] = s / bs[d] < nb[d] ? s / bs[d] : nb[d] - 1;
     }
     bin[j] = bidx[0] + nb[0] * (bidx[1] + nb[1] * bidx[2]);
     cnt[bin[j] + 1]++;

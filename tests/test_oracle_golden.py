@@ -181,3 +181,29 @@ def test_oracle_spread_on_a_given_grid_matches_numpy(grid):
     lhs = np.vdot(g.ravel(), got.ravel())
     rhs = np.vdot(back, c)
     assert abs(lhs - rhs) <= 1e-9 * abs(lhs)
+
+
+@pytest.mark.parametrize("modes,ns", [((60, 50), 8), ((60, 50), 13), ((40, 33), 11), ((16, 18, 14), 10),
+                                      ((300,), 9)])
+def test_oracle_spread_independent_of_threads(modes, ns):
+    # The coloured bin schedule must be race-free: every cell receives its
+    # additions in the same order whatever the thread count, so a serial and
+    # a parallel spread agree bit for bit.  Grids whose last bin is narrower
+    # than ns - 1 cells (nf 100 with 32-cell bins) once let the halo of the
+    # bin before it wrap into bin 0 while bin 0 was being spread.
+    rng = np.random.default_rng(ns)
+    dim = len(modes)
+    plan = O.OraclePlan(1, modes, 1, 1.01 * 10.0 ** (1 - ns), False)
+    assert plan.ns == ns
+    M = 6000
+    pts = [rng.uniform(-np.pi, np.pi, M) for _ in range(dim)] + [None] * (3 - dim)
+    c = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    nthr = O.num_threads()
+    try:
+        O.set_num_threads(1)
+        serial = plan.spread(*pts, c)
+        O.set_num_threads(max(4, nthr))
+        parallel = plan.spread(*pts, c)
+    finally:
+        O.set_num_threads(nthr)
+    assert np.array_equal(serial, parallel)
