@@ -71,7 +71,8 @@ class PlanInfo(ctypes.Structure):
         "type", "dim", "ms", "mt", "mu", "nf1", "nf2", "nf3", "ns", "M", "ntransf",
         "maxbatchsize", "method", "sort", "binsizex", "binsizey", "binsizez", "nbins",
         "nsubprob", "kerevalmeth")] + [("beta", c_double), ("es_c", c_double),
-                                       ("line_fft", c_int), ("cell_order", c_int)]
+                                       ("line_fft", c_int), ("cell_order", c_int),
+                                       ("width_rule", c_int)]
 
 
 CufinufftPlan = c_void_p
@@ -149,6 +150,10 @@ _stage_times.restype = c_int
 _stage_timesf = lib.cufinufftf_stage_times
 _stage_timesf.argtypes = [c_void_p, c_double_p, ctypes.POINTER(ctypes.c_longlong), c_int]
 _stage_timesf.restype = c_int
+_set_width_rule = lib.cufinufft_set_width_rule
+_set_width_rule.argtypes = [c_int, c_int_p]
+_set_width_rule.restype = c_int
+
 _batch_make = lib.cufinufft_batch_make
 _batch_make.argtypes = [c_int, ctypes.POINTER(c_void_p), ctypes.POINTER(c_void_p)]
 _batch_make.restype = c_int

@@ -21,7 +21,7 @@ from cufinufft_gb300._cufinufft import (NufftOpts, PlanInfo, _default_opts, _des
                                         _destroy_planf, _exec_plan, _exec_planf, _get_info,
                                         _get_infof, _make_plan, _make_planf, _set_pts, _set_ptsf,
                                         _set_stream, _set_streamf, _set_timing, _set_timingf,
-                                        _stage_times, _stage_timesf)
+                                        _set_width_rule, _stage_times, _stage_timesf)
 
 # If Python is shutting down, __del__ does nothing (as in the reference).
 exiting = False
@@ -81,7 +81,10 @@ class cufinufft:
     :param eps: requested relative tolerance.
     :param isign: sign of the exponent; default +1 for type 1, -1 for type 2.
     :param dtype: np.float32 or np.float64 (selects the FP32/FP64 library).
-    :param kwargs: fields of the options struct (e.g. gpu_method=2).
+    :param kwargs: fields of the options struct (e.g. gpu_method=2), and the
+        extension ``width_rule``: "reference" (the default: the reference's
+        kernel width for eps) or "tol" (the narrowest width whose measured
+        error meets eps; see cufinufft_set_width_rule).
     """
 
     def __init__(self, nufft_type, modes, n_trans=1, eps=1e-6, isign=None, dtype=np.float32,
@@ -119,6 +122,10 @@ class cufinufft:
         self.eps = float(eps)
         self.n_trans = n_trans
         self._maxbatch = kwargs.pop("maxbatchsize", 1)
+        rule = kwargs.pop("width_rule", None)
+        if rule not in (None, "reference", "tol", 0, 1):
+            raise TypeError(f"Invalid width_rule '{rule}'")
+        self._width_rule = None if rule is None else (1 if rule in ("tol", 1) else 0)
 
         modes = tuple(modes)[::-1] + (1,) * (3 - self.dim)
         self.modes = (c_int * 3)(*modes)
@@ -142,8 +149,16 @@ class cufinufft:
 
     def _plan(self):
         self.plan = c_void_p(None)
-        ier = self._make_plan(self._finufft_type, self.dim, self.modes, self.isign, self.n_trans,
-                              self.eps, self._maxbatch, byref(self.plan), self.opts)
+        prev = c_int(-1)
+        if self._width_rule is not None:
+            _set_width_rule(self._width_rule, byref(prev))
+        try:
+            ier = self._make_plan(self._finufft_type, self.dim, self.modes, self.isign,
+                                  self.n_trans, self.eps, self._maxbatch, byref(self.plan),
+                                  self.opts)
+        finally:
+            if self._width_rule is not None:
+                _set_width_rule(prev.value, None)
         if ier != 0:
             raise RuntimeError('Error creating plan.')
 

@@ -142,6 +142,9 @@ template <typename T> static void release(Plan<T>* p) {
   p->cap_sub_dense = 0;
   if (p->h_total) cudaFreeHost(p->h_total);
   p->h_total = nullptr;
+  if (p->h_status) cudaFreeHost(p->h_status);
+  p->h_status = nullptr;
+  p->d_status = nullptr;
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
   for (cudaEvent_t e : p->ev_live) cudaEventDestroy(e);
   p->ev_pool.clear();
@@ -419,18 +422,39 @@ static std::vector<LineArgs<T>> line_passes(const Plan<T>* p, cplx_t<T>* fk, int
 
 static int max_smem_optin(int device);
 
+// Kernel-width rule of the next makeplan calls on this thread (-1: from
+// CUFINUFFT_WIDTH_RULE, "tol" or "1" for the tolerance-meeting rule, else
+// the reference's).
+static thread_local int t_width_rule = -1;
+
+static int width_rule_now() {
+  if (t_width_rule >= 0) return t_width_rule;
+  const char* v = std::getenv("CUFINUFFT_WIDTH_RULE");
+  if (v && (std::strcmp(v, "tol") == 0 || std::strcmp(v, "1") == 0)) return 1;
+  return 0;
+}
+
+static int set_width_rule(int rule, int* previous) {
+  if (rule < -1 || rule > 1) return CUFINUFFT_ERR_ARG;
+  if (previous) *previous = t_width_rule;
+  t_width_rule = rule;
+  return 0;
+}
+
 template <typename T>
 static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int iflag, int ntransf,
                          double tol, int maxbatchsize, const cufinufft_opts* opts) {
   p->type = type;
   p->dim = dim;
+  p->width_rule = width_rule_now();
   if (const char* v = std::getenv("CUFINUFFT_KERNEL_VARIANT")) {
     const int k = std::atoi(v);
     p->variant = (k == 1 || k == 2) ? k : 0;
   }
   if (opts) p->opts = *opts;
   else default_opts(type, dim, &p->opts);
-  int ier = setup_spreader(tol, p->opts.upsampfac, p->opts.gpu_kerevalmeth, is_single<T>(), &p->sp);
+  int ier = setup_spreader(tol, p->opts.upsampfac, p->opts.gpu_kerevalmeth, is_single<T>(), &p->sp,
+                           p->width_rule, dim);
   if (ier > 1) return ier;
   for (int k = 0; k < dim; ++k) p->N[k] = nmodes[k];
   setup_binsize(dim, &p->opts);
@@ -514,6 +538,12 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   CFG_CUDA(cudaStreamCreate(&p->own));  // blocking: ordered after the legacy default stream
   p->stream = p->own;
   CFG_CUDA(cudaMallocHost(&p->h_total, sizeof(int)));
+  if (type == 2) {
+    CFG_CUDA(cudaHostAlloc(&p->h_status, 2 * sizeof(int), cudaHostAllocMapped));
+    p->h_status[0] = p->h_status[1] = 0;
+    CFG_CUDA(cudaHostGetDevicePointer(&p->d_status, p->h_status, 0));
+    if (const char* v = std::getenv("CUFINUFFT_TMA_WAIT_TEST")) p->tma_wait_test = v[0] == '1';
+  }
 
   const long long Nf = grid_cells(p);
   CFG_CUDA(cudaMalloc(&p->count, sizeof(int) * (size_t)p->nbins));
@@ -899,8 +929,24 @@ static bool graphs_enabled() {
 // removes most of the gaps between its kernels.  A plan stream that is already
 // being captured (a batch recording this plan), or a capture that fails, runs
 // the kernels directly.
+// A tile wait of an earlier execute ran out (SpreadArgs::status): its result
+// was still computed from the same values, but the stall is reported once,
+// as a CUDA error of the next execute or stage-time read (the flag is
+// cleared).
+template <typename T>
+static int take_status(Plan<T>* p) {
+  if (!p->h_status) return 0;
+  volatile int* s = p->h_status;
+  if (s[0] == 0 && s[1] == 0) return 0;
+  if (s[1]) fprintf(stderr, "cufinufft: an interpolation tile copy did not complete\n");
+  else fprintf(stderr, "cufinufft: an interpolation tile wait ran out (tile loaded cell by cell)\n");
+  s[0] = s[1] = 0;
+  return CUFINUFFT_ERR_CUDA;
+}
+
 template <typename T>
 static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
+  if (const int e = take_status(p)) return e;
   if (p->timing || !p->planned || !graphs_enabled()) return execute_direct(p, c, fk);
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(p->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
@@ -980,6 +1026,7 @@ static void fill_info(const Plan<T>* p, cufinufft_plan_info* info) {
   info->es_c = p->sp.c;
   info->line_fft = p->line_fft ? 1 : 0;
   info->cell_order = p->cell_order ? 1 : 0;
+  info->width_rule = p->width_rule;
 }
 
 // ---------------------------------------------------------------------------
@@ -1467,6 +1514,8 @@ static int stage_times_entry(H* h, double* ms, long long* batches, int reset) {
   DeviceGuard g(h->p.device);
   int e = cfg::collect_times(&h->p);
   if (e) return e;
+  e = cfg::take_status(&h->p);
+  if (e) return e;
   for (int k = 0; k < 3; ++k) ms[k] = h->p.stage_ms[k];
   if (batches) *batches = h->p.stage_batches;
   if (reset) {
@@ -1599,6 +1648,8 @@ int cufinufftf_set_layout_class(cufinufftf_plan plan, int cls) {
   DeviceGuard g(plan->p.device);
   return cfg::apply_layout_class(&plan->p, cls);
 }
+
+int cufinufft_set_width_rule(int rule, int* previous) { return cfg::set_width_rule(rule, previous); }
 
 int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info) {
   if (!plan || !info) return CUFINUFFT_ERR_GENERIC;

@@ -59,7 +59,10 @@ std::mutex g_na_mutex;
 void* g_na_base[kNaMaxDevices] = {};
 
 // Device address of the scratch array on the current device (looked up once
-// per device; the host-side name is only a stand-in for the symbol).
+// per device; the host-side name is only a stand-in for the symbol).  The
+// address is cached for the life of the process: a device reset after the
+// first call would reload the module and leave the cached address stale, so
+// resets are not supported once the entry point has been used.
 cudaError_t scratch_base(int dev, unsigned char** out) {
   if (dev < 0 || dev >= kNaMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_na_mutex);

@@ -95,6 +95,12 @@ template <typename T> struct SpreadArgs {
   int variant;              // kernel family: 0 default, 1 one thread per point, 2 warp-cooperative
   int run;                  // method 2 spreading over cell-ordered points (cell-run kernel)
   const unsigned char* sub_dense;  // run: subproblems that start on a dense cell
+  // Interpolation tile waits (bulk copies): status[0] is set when a wait ran
+  // out and the tile was loaded cell by cell instead, status[1] when the copy
+  // had still not landed after a second full wait.  Host-mapped memory the
+  // next call on the plan reads; null: not recorded.
+  int* status;
+  int tma_wait_test;        // nonzero: every tile's first wait gives up at once (tests)
 };
 
 // Cells of one subproblem tile: the bin plus the ns-1 cells its points

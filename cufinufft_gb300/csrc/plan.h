@@ -23,6 +23,7 @@ template <typename T> struct Plan {
   int ntransf = 1, maxbatch = 1, iflag = 1;
   cufinufft_opts opts;
   SpreaderParams sp{};
+  int width_rule = 0;  // 0: the reference's kernel width, 1: the tolerance-meeting width
   int method = 0;  // method run: 1 (NU-point driven) or 2 (subproblem); 0 = invalid
                    // (layout method 5 = method 2 with cell_order, see set_layout)
   int variant = 0; // kernel family: 0 default, 1 one thread per point, 2 warp-cooperative
@@ -73,6 +74,10 @@ template <typename T> struct Plan {
   unsigned char* sub_dense = nullptr;  // per subproblem: starts on a dense cell (cell order)
   size_t cap_sub_dense = 0;
   int* h_total = nullptr;  // pinned readback of the subproblem count
+  // interpolation tile-wait status (SpreadArgs::status): host-mapped, two ints
+  int* h_status = nullptr;
+  int* d_status = nullptr;
+  int tma_wait_test = 0;   // CUFINUFFT_TMA_WAIT_TEST=1 at makeplan
   // execute as a CUDA graph (timing off): captured for one pair of caller
   // arrays and one plan state (`version` counts setpts / set_layout)
   cudaGraph_t graph = nullptr;
@@ -191,6 +196,8 @@ inline SpreadArgs<T> spread_args(Plan<T>* p) {
   a.variant = p->variant;
   a.run = (p->cell_order && p->type == 1 && p->method == 2) ? 1 : 0;
   a.sub_dense = a.run ? p->sub_dense : nullptr;
+  a.status = p->d_status;
+  a.tma_wait_test = p->tma_wait_test;
   return a;
 }
 

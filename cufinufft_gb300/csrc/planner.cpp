@@ -5,12 +5,55 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 
 namespace cfg {
 
-int setup_spreader(double tol, double upsampfac, int kerevalmeth, bool single, SpreaderParams* sp) {
+// Worst relative l2 error of the FP64 oracle against direct sums, divided by
+// the reference's accuracy model for the width (10^(1-ns) at upsampfac 2,
+// exp(-pi ns sqrt(1 - 1/upsampfac)) otherwise), over uniform random points,
+// types 1 and 2, two mode shapes and three seeds per dimension; rows ns =
+// 2..16, columns dim 1..3.  Printed by oracle/width_table.py.
+static const double kWidthErr2[15][3] = {
+    {0.6, 0.837, 0.97},   {0.696, 0.968, 1.24}, {1.58, 2.07, 2.79}, {0.725, 1.06, 1.72},
+    {0.703, 1.04, 1.69},  {0.872, 1.21, 1.44},  {1.11, 1.48, 1.39}, {1.31, 1.86, 2.14},
+    {1.48, 2.17, 3.45},   {1.46, 2.07, 3.74},   {1.54, 2.25, 3.54}, {1.78, 2.45, 2.65},
+    {2.84, 3.02, 2.7},    {17.7, 3.98, 4.23},   {166, 14.6, 12}};
+static const double kWidthErr125[15][3] = {
+    {2.63, 3.61, 4},      {2.7, 3.88, 3.95},    {2.85, 4.56, 4.31}, {2.96, 3.52, 4.73},
+    {2.23, 3.09, 4.56},   {1.81, 2.87, 3.29},   {2.21, 2.94, 2.12}, {2.77, 3.32, 2.21},
+    {3.31, 4.27, 4.41},   {3.52, 4.42, 5.18},   {2.92, 6.16, 5.77}, {2.86, 5.57, 5.81},
+    {2.47, 4.52, 3.76},   {2.87, 4.04, 1.83},   {3.82, 4.5, 1.32}};
+
+double width_error_bound(int ns, int dim, double upsampfac) {
+  if (ns < 2 || ns > kMaxNS || dim < 1 || dim > 3) return 1.0;
+  const double model = upsampfac == 2.0 ? std::pow(10.0, 1 - ns)
+                                        : std::exp(-M_PI * ns * std::sqrt(1.0 - 1.0 / upsampfac));
+  const double r = (upsampfac == 2.0 ? kWidthErr2 : kWidthErr125)[ns - 2][dim - 1];
+  return 1.25 * r * model;  // a quarter of margin over the worst case measured
+}
+
+int width_for_tol(double tol, int dim, double upsampfac, bool single, int* warn) {
+  // the widest kernel the reference's own rule uses in this precision (its
+  // width at the machine-precision floor, contrib/spreadinterp.cpp:35-49)
+  SpreaderParams cap;
+  setup_spreader(0.0, upsampfac, 0, single, &cap);
+  for (int ns = 2; ns <= cap.ns; ++ns)
+    if (width_error_bound(ns, dim, upsampfac) <= tol) return ns;
+  if (warn) *warn = 1;
+  return cap.ns;
+}
+
+int setup_spreader(double tol, double upsampfac, int kerevalmeth, bool single, SpreaderParams* sp,
+                   int width_rule, int dim) {
   if (upsampfac != 2.0) {
-    if (kerevalmeth == 1) return 8;   // HORNER_WRONG_BETA (no fitted table for sigma != 2)
+    // HORNER_WRONG_BETA: the reference has no polynomial table for sigma !=
+    // 2; the fitted polynomials here serve any sigma unless the reference's
+    // refusal is asked for (CUFINUFFT_HORNER_SIGMA2_ONLY=1)
+    if (kerevalmeth == 1) {
+      const char* v = std::getenv("CUFINUFFT_HORNER_SIGMA2_ONLY");
+      if (v && v[0] == '1') return 8;
+    }
     if (upsampfac <= 1.0) return 7;   // ERR_UPSAMPFAC_TOO_SMALL
   }
   int ier = 0, ns;
@@ -27,6 +70,7 @@ int setup_spreader(double tol, double upsampfac, int kerevalmeth, bool single, S
     }
     if (ns < 2) ns = 2;
     if (ns > kMaxNS) { ns = kMaxNS; ier = 1; }
+    if (width_rule == 1) ns = width_for_tol(tol, dim, upsampfac, true, &ier);
     const float cf = (float)(4.0 / (double)(float)(ns * ns));
     float bon = 2.30f;
     if (ns == 2) bon = 2.20f;
@@ -46,6 +90,7 @@ int setup_spreader(double tol, double upsampfac, int kerevalmeth, bool single, S
     if (upsampfac != 2.0) ns = (int)std::ceil(-std::log(eps) / (M_PI * std::sqrt(1.0 - 1.0 / upsampfac)));
     if (ns < 2) ns = 2;
     if (ns > kMaxNS) { ns = kMaxNS; ier = 1; }
+    if (width_rule == 1) ns = width_for_tol(tol, dim, upsampfac, false, &ier);
     c = 4.0 / (double)(ns * ns);
     double bon = 2.30;
     if (ns == 2) bon = 2.20;

@@ -211,6 +211,7 @@ __device__ __forceinline__ void tile_flush(const cplx_t<T>* tile, cplx_t<T>* gri
 
 // Polls of the tile barrier before a thread gives up on the bulk copy and
 // loads its share of the tile itself (the data is the same either way).
+// Each poll may itself wait a short, hardware-chosen time.
 constexpr int kTmaWaitPolls = 1 << 20;
 
 // Tile row length (cells) of a bulk-copied tile: a box row must be a
@@ -237,13 +238,23 @@ __device__ __forceinline__ void tile_copy_start(cplx_t<T>* tile, const CUtensorM
   else tma_load4(tile, map, 2 * st.ox, st.oy, st.oz, t, bar);
 }
 
-// Every thread: wait for the bulk copy; a thread whose wait runs out loads
-// its share of the tile cell by cell instead (the same values; the caller
-// syncs the block afterwards).
+// Every thread: wait for the bulk copy.  A thread whose wait runs out
+// records it in status[0] (the next call on the plan returns an error) and
+// loads its share of the tile cell by cell, which writes the values the copy
+// writes; it then waits for the copy once more, so that the block does not
+// retire -- and its shared memory go to another block -- while the copy may
+// still write into it.  A copy still missing after that second wait is
+// recorded in status[1].  `test` makes the first wait give up at once.
+__device__ __forceinline__ void status_set(int* status, int k) {
+  if (status) *reinterpret_cast<volatile int*>(status + k) = 1;
+}
 template <typename T>
 __device__ __forceinline__ void tile_copy_wait(cplx_t<T>* tile, unsigned long long* bar, const cplx_t<T>* grid,
-                                               const SubTile& st, const GridGeom& g) {
-  if (!mbar_wait(bar, 0, kTmaWaitPolls)) tile_load_periodic<T>(tile, grid, st, g);
+                                               const SubTile& st, const GridGeom& g, int* status, int test) {
+  if (mbar_wait(bar, 0, test ? 0 : kTmaWaitPolls)) return;
+  status_set(status, 0);
+  tile_load_periodic<T>(tile, grid, st, g);
+  if (!mbar_wait(bar, 0, kTmaWaitPolls)) status_set(status, 1);
 }
 
 // Host: encode the tensor map of `ntr` fine grids at `grid` for tiles of a
@@ -557,7 +568,7 @@ k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) 
   InterpPoint<T, DIM, NS> pt;
   if (!bulk) tile_load_periodic<T>(tile, src, st, a.g);
   if (p < p_end) pt.fetch(a, p, st);
-  if (bulk) tile_copy_wait<T>(tile, &tile_bar, src, st, a.g);
+  if (bulk) tile_copy_wait<T>(tile, &tile_bar, src, st, a.g, a.status, a.tma_wait_test);
   __syncthreads();
   if (p >= p_end) return;
   pt.rows(a);

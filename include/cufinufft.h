@@ -109,9 +109,25 @@ typedef struct cufinufft_plan_info {
   double beta, es_c;
   int line_fft;   /* 1: pruned line FFTs (fftpass.cu), 0: cuFFT over the whole grid */
   int cell_order; /* 1: method 2 spreading over cell-ordered points (cell-run kernel) */
+  int width_rule; /* kernel-width rule the plan was made under (cufinufft_set_width_rule) */
 } cufinufft_plan_info;
 int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info);
 int cufinufftf_get_info(cufinufftf_plan plan, cufinufft_plan_info* info);
+
+/* Kernel-width rule (no counterpart in the reference; it sets no field of
+ * cufinufft_opts, whose layout is the reference's).  The reference picks
+ * ns = ceil(-log10(tol/10)) at upsampfac 2 (contrib/spreadinterp.cpp:42),
+ * which leaves relative l2 errors of one to four times tol.  Rule 1 picks
+ * the narrowest width whose error, as measured with an FP64 restatement of
+ * the algorithm against direct sums (uniform random points and data, the
+ * plan's dimension, with a 25% margin), is at most tol -- usually one more
+ * than the reference's width -- and never wider than the reference's width
+ * at the precision's machine epsilon.  Rule 0 is the reference's (the
+ * default).  The rule applies to the makeplan calls that follow on the
+ * calling thread; -1 returns to the process default, which the environment
+ * variable CUFINUFFT_WIDTH_RULE ("tol" or "1": rule 1) sets.  *previous
+ * (when not NULL) receives the thread's earlier setting. */
+int cufinufft_set_width_rule(int rule, int* previous);
 
 /* Stage timing.  With timing on, execute() records CUDA events around its
  * three stages on the plan stream; stage_times() waits for them and returns
@@ -214,15 +230,20 @@ int cufinufftf_batch_destroy(cufinufftf_batch batch);
  * a framework that owns all device memory, real-time loops, memory-budgeted
  * services): spreads M points (x, y in [-3pi, 3pi), strengths c, all device
  * arrays) onto the caller's nf1 x nf2 fine grid fw (x fastest), which this
- * call zeroes first, with the ES kernel of FP32 tolerance tol -- the type-1
- * spreading stage of a plan with that fine grid (bin sort, 32x32 bins,
- * shared-memory subproblems) -- on `stream`, without allocating: its sort
- * scratch is a fixed device array of about 3.2 MB that every GPU loading
- * the library holds.  Limits: M <= 131072 and at most 4096 bins (fine grids
- * up to 2048 x 2048); larger requests return CUFINUFFT_ERR_ARG.  All calls on
- * a device share that scratch: calls whose GPU work overlaps race and must be
- * serialised by the caller.  The first call on each device looks up the
- * scratch address, so make it before any stream capture. */
+ * call zeroes first, with the ES kernel of FP32 tolerance tol, on `stream`,
+ * without allocating.  It runs the type-1 spreading stage of a plan with
+ * that fine grid (bin sort, 32x32 bins, shared-memory subproblems) in plain
+ * bin order and always evaluates the ES kernel directly (exp form, not the
+ * fitted polynomials), so its grid matches that plan's spreading within
+ * FP32 rounding, not bit for bit.  Its sort scratch is a fixed device array
+ * of about 3.2 MB that every GPU loading the library holds.  Limits:
+ * M <= 131072 and at most 4096 bins (fine grids up to 2048 x 2048); larger
+ * requests return CUFINUFFT_ERR_ARG.  All calls on a device share that
+ * scratch: calls whose GPU work overlaps race and must be serialised by the
+ * caller.  The first call on each device looks up the scratch address, so
+ * make it before any stream capture; the address is kept for the life of
+ * the process, so a device reset (cudaDeviceReset) after that first call is
+ * not supported. */
 int cufinufftf_spread2d_noalloc(int M, const float* x, const float* y, const cuFloatComplex* c,
                                 int nf1, int nf2, float tol, cuFloatComplex* fw,
                                 cudaStream_t stream);

@@ -132,6 +132,16 @@ def fseries(nf: int, ns: int, beta: float, c: float) -> np.ndarray:
     return out
 
 
+def tol_for_width(ns: int, upsampfac: float = 2.0) -> float:
+    """A tolerance for which setup_spreader (contrib/spreadinterp.cpp:29-45)
+    chooses kernel width ns: ns = ceil(-log10(tol/10)) at upsampfac 2,
+    ceil(-ln(tol) / (pi sqrt(1 - 1/upsampfac))) otherwise."""
+    if upsampfac == 2.0:
+        return 1.01 * 10.0 ** (1 - ns)
+    import math
+    return math.exp(-(ns - 0.5) * math.pi * math.sqrt(1.0 - 1.0 / upsampfac))
+
+
 class OraclePlan:
     """FP64 restatement of a cuFINUFFT type-1/2 plan (test infrastructure).
 
@@ -142,21 +152,29 @@ class OraclePlan:
     """
 
     def __init__(self, nufft_type: int, modes, iflag: int, tol: float, single: bool,
-                 gpu_method: int = 0, obin: tuple = (8, 8, 8), spreadinterponly: bool = False):
+                 gpu_method: int = 0, obin: tuple = (8, 8, 8), spreadinterponly: bool = False,
+                 upsampfac: float = 2.0, ns: int | None = None):
         self.type = int(nufft_type)
         self.modes = tuple(int(m) for m in modes)
         self.dim = len(self.modes)
         self.iflag = 1 if iflag >= 0 else -1
-        ier, self.ns, self.beta, self.c = setup_spreader(tol, single)
+        self.upsampfac = float(upsampfac)
+        if ns is not None:
+            # a given kernel width (a plan made under another width rule):
+            # the same shape formulas at that width
+            tol = tol_for_width(int(ns), self.upsampfac)
+        ier, self.ns, self.beta, self.c = setup_spreader(tol, single, self.upsampfac)
         if ier > 1:
             raise ValueError(f"setup_spreader error {ier}")
+        if ns is not None and self.ns != int(ns):
+            raise ValueError(f"width {ns} not reachable ({self.ns})")
         if spreadinterponly:
             # the grid is the modes array itself (the reference's spread /
             # interp tests set gpu_spreadinterponly and pass nf directly,
             # test/spread2d_test.cu:80,133)
             self.nf = self.modes
         else:
-            self.nf = tuple(set_nf_type12(m, self.ns, gpu_method, obin[d])
+            self.nf = tuple(set_nf_type12(m, self.ns, gpu_method, obin[d], self.upsampfac)
                             for d, m in enumerate(self.modes))
         self.ker = [fseries(nf, self.ns, self.beta, self.c) for nf in self.nf]
 

@@ -64,10 +64,12 @@ def run_gpu(ntype, modes, pts, data, tol, single, ntr=1, iflag=None, **opts):
     return out, info
 
 
-def oracle_nufft(ntype, modes, pts, data, tol, single, ntr=1, iflag=None, gpu_method=1):
+def oracle_nufft(ntype, modes, pts, data, tol, single, ntr=1, iflag=None, gpu_method=1, **plan_kw):
+    """The oracle's transform; ``plan_kw`` passes ``ns`` (a plan's kernel
+    width under another width rule) or ``upsampfac`` to the oracle plan."""
     if iflag is None:
         iflag = 1 if ntype == 1 else -1
-    plan = O.OraclePlan(ntype, modes, iflag, tol, single, gpu_method=gpu_method)
+    plan = O.OraclePlan(ntype, modes, iflag, tol, single, gpu_method=gpu_method, **plan_kw)
     args = list(pts) + [None] * (3 - len(pts))
     return plan.execute(*args, data=data, ntr=ntr)
 

@@ -3,6 +3,7 @@
 v1.3), plus the stage-repetition and error-return behaviour of the C ABI
 (docs/cppdoc.md:3-8 of the reference)."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -220,8 +221,9 @@ def test_c_abi_error_returns():
     plan = ctypes.c_void_p(None)
     assert mk(1, 2, nmodes, 1, 1, 1e-12, 0, ctypes.byref(plan), None) == 0
     assert de(plan) == 0
-    # upsampfac <= 1 is error 7; Horner with sigma != 2 is error 8
-    # (contrib/spreadinterp.cpp:14-26)
+    # upsampfac <= 1 is error 7 (contrib/spreadinterp.cpp:19-22).  Horner with
+    # sigma != 2 is the reference's error 8 (:14-18) only on request: the
+    # fitted polynomials here serve any sigma
     opts = L.NufftOpts()
     L._default_optsf(1, 2, opts)
     opts.upsampfac = 0.9
@@ -230,26 +232,42 @@ def test_c_abi_error_returns():
     de(plan)
     opts.upsampfac = 1.25
     opts.gpu_kerevalmeth = 1
+    os.environ["CUFINUFFT_HORNER_SIGMA2_ONLY"] = "1"
+    try:
+        plan = ctypes.c_void_p(None)
+        assert mk(1, 2, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), opts) == 8
+        de(plan)
+    finally:
+        del os.environ["CUFINUFFT_HORNER_SIGMA2_ONLY"]
     plan = ctypes.c_void_p(None)
-    assert mk(1, 2, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), opts) == 8
-    de(plan)
+    assert mk(1, 2, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), opts) == 0
+    assert de(plan) == 0
 
 
-def test_upsampfac_125():
+@pytest.mark.parametrize("kerevalmeth", [0, 1])
+@pytest.mark.parametrize("ntype", [1, 2])
+def test_upsampfac_125(kerevalmeth, ntype):
     # sigma = 1.25 takes the reference's custom width/beta formulas
-    # (contrib/spreadinterp.cpp:40-61); results still meet the tolerance
+    # (contrib/spreadinterp.cpp:40-61), with the exp kernel or the fitted
+    # polynomials (which the reference refuses at sigma != 2); results match
+    # the oracle's restatement at sigma 1.25 and meet the tolerance
     for single, tol in ((True, 1e-4), (False, 1e-8)):
-        rng = np.random.default_rng(9)
+        rng = np.random.default_rng(9 + ntype)
         modes = (30, 26)
         dt = np.float32 if single else np.float64
-        pts = NC.points(rng, 2, 2000, dtype=dt)
-        c = NC.strengths(rng, 2000)
-        out, info = NC.run_gpu(1, modes, pts, c, tol, single, upsampfac=1.25)
-        idx = np.arange(int(np.prod(modes)))
-        d = NC.direct(1, modes, [p.astype(np.float64) for p in pts], c[0], 1, idx)
+        pts = NC.points(rng, 2, 2000, dtype=dt, edges=False)
+        data = NC.strengths(rng, 2000) if ntype == 1 else NC.coeffs(rng, modes)
+        out, info = NC.run_gpu(ntype, modes, pts, data, tol, single, upsampfac=1.25,
+                               gpu_kerevalmeth=kerevalmeth)
+        p64 = [p.astype(np.float64) for p in pts]
+        idx = np.arange(out.size)
+        d = NC.direct(ntype, modes, p64, data.reshape(-1), 1 if ntype == 1 else -1, idx)
         err = np.linalg.norm(out.ravel() - d) / np.linalg.norm(d)
         assert err < 5 * max(tol, 2e-5 if single else 0), (err, info)
         assert info["nf1"] < 2 * 30
+        ref = NC.oracle_nufft(ntype, modes, p64, data, tol, single, upsampfac=1.25)
+        same = np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
+        assert same < (2e-5 if single else max(1e-10, tol if kerevalmeth else 0)), same
 
 
 def test_type2_padding_stays_zero_across_executes():

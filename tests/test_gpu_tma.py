@@ -53,3 +53,45 @@ def test_bulk_copy_tiles_against_oracle(monkeypatch):
     ref = NC.oracle_nufft(2, modes, pts, fk, 1e-6, True)
     err = np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
     assert err < 1e-5, err
+
+
+@pytest.mark.parametrize("single", [True, False])
+def test_tile_wait_timeout_reported(monkeypatch, single):
+    """A tile wait that runs out is recorded, its tile is loaded cell by cell
+    (same values, so the result is right), the block waits for the copy
+    before it retires, and the next call on the plan returns the CUDA error
+    code once.  CUFINUFFT_TMA_WAIT_TEST=1 makes every first wait give up at
+    once; the second wait is the normal bounded one, which the copy meets."""
+    import torch
+
+    from cufinufft_gb300 import cufinufft
+    monkeypatch.setenv("CUFINUFFT_TMA", "1")
+    monkeypatch.setenv("CUFINUFFT_TMA_WAIT_TEST", "1")
+    rng = np.random.default_rng(8)
+    modes = (96, 80)
+    dt = np.float32 if single else np.float64
+    tol = 1e-6 if single else 1e-9
+    pts = NC.points(rng, 2, 6000, dtype=dt)
+    fk = NC.coeffs(rng, modes)
+    plan = cufinufft(2, modes[::-1], eps=tol, dtype=dt, gpu_method=2)
+    plan.set_pts(*[torch.from_numpy(p).cuda() for p in pts[::-1]])
+    fk_d = torch.from_numpy(fk.astype(plan.complex_dtype)).cuda()
+    c_d = torch.zeros((1, pts[0].size), dtype=fk_d.dtype, device="cuda")
+    plan.execute(c_d, fk_d)
+    torch.cuda.synchronize()
+    ref = NC.oracle_nufft(2, modes, [p.astype(np.float64) for p in pts], fk, tol, single)
+    out = c_d.cpu().numpy()
+    err = np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
+    assert err < (1e-5 if single else 1e-10), err
+    # the stall is reported by the next call, once
+    with pytest.raises(RuntimeError):
+        plan.execute(c_d, fk_d)
+    monkeypatch.setenv("CUFINUFFT_TMA_WAIT_TEST", "0")
+    plan2 = cufinufft(2, modes[::-1], eps=tol, dtype=dt, gpu_method=2)
+    plan2.set_pts(*[torch.from_numpy(p).cuda() for p in pts[::-1]])
+    plan2.execute(c_d, fk_d)
+    torch.cuda.synchronize()
+    plan2.execute(c_d, fk_d)  # no stall recorded: no error
+    torch.cuda.synchronize()
+    assert np.array_equal(c_d.cpu().numpy(), out)
+    del plan, plan2

@@ -30,20 +30,24 @@ def _entry():
     return fn
 
 
-def test_noalloc_spread_matches_plan_execute_twice():
+@pytest.mark.parametrize("modes,span", [
+    ((96, 80), 1),    # fine grid 192 x 160: whole 32-cell bins, points in [-pi, pi)
+    ((50, 70), 3),    # fine grid 100 x 140: partial last bins (periodic wrap of
+                      # their tiles), points in [-3pi, 3pi) (the fold)
+])
+def test_noalloc_spread_matches_plan_execute_twice(modes, span):
     import torch
 
     from cufinufft_gb300 import cufinufft
     from oracle import oracle as O
 
     spread = _entry()
-    modes = (96, 80)          # (N1, N2), N1 fastest
-    tol = 1e-5
+    tol = 1e-5                # modes are (N1, N2), N1 fastest
     stream = torch.cuda.current_stream()
     for call, (M, seed) in enumerate(((20000, 1), (7000, 2))):
-        rng = np.random.default_rng(seed)
-        x = rng.uniform(-np.pi, np.pi, M).astype(np.float32)
-        y = rng.uniform(-np.pi, np.pi, M).astype(np.float32)
+        rng = np.random.default_rng(seed + 10 * span)
+        x = rng.uniform(-span * np.pi, span * np.pi, M).astype(np.float32)
+        y = rng.uniform(-span * np.pi, span * np.pi, M).astype(np.float32)
         c = (rng.standard_normal(M) + 1j * rng.standard_normal(M)).astype(np.complex64)
         xg, yg, cg = (torch.from_numpy(a).cuda() for a in (x, y, c))
 
