@@ -11,9 +11,15 @@ cluster3d (3D type 1, 128^3 modes, M = 3.2e7, half uniform and half in 8
 Gaussian clusters of sigma 0.05, FP32, tol 1e-6) and cluster3d-f64 (3D type 2
 on the same points, FP64, tol 1e-9).
 
-Metric: nonuniform points per second of execute(), with the relative l2
-error against the FP64 oracle (direct sum on random modes/targets) reported
-beside it.  `value` times execute() on device-resident inputs with CUDA events
+Metric: nonuniform points per second of execute() at relative l2 error <= tol
+against FP64 direct sums on random modes/targets (the error is reported
+beside it).  Plans use the library's tolerance-meeting kernel width
+(--width-rule tol, the default): the reference's own width rule
+ns = ceil(-log10(tol/10)) leaves errors of one to four times tol, so its
+throughput is reported beside the headline as `parity_width`, and --width-rule
+reference times it instead.  The default run also times, device time only,
+the 3D clustered type-1 workload and the uneven 64-plan batch (tuned+batched
+against 64 plain plans) under `extra_workloads` (--no-extras skips them).  `value` times execute() on device-resident inputs with CUDA events
 on the plan's stream (L2 flushed with a 256 MB write between steps, outside
 the timed events); `e2e` times the same public call with the input copied
 from pinned host memory and the output copied back inside each step.
@@ -243,10 +249,10 @@ def committed_traffic(key: str):
 
 
 # --------------------------------------------------------------------------
-def oracle_plan(w: Workload, cores: int):
+def oracle_plan(w: Workload, cores: int, ns=None):
     from oracle import oracle as O
     O.set_num_threads(cores)
-    plan = O.OraclePlan(w.ntype, w.modes, 1 if w.ntype == 1 else -1, w.tol, w.single)
+    plan = O.OraclePlan(w.ntype, w.modes, 1 if w.ntype == 1 else -1, w.tol, w.single, ns=ns)
     plan.fft_workers = cores
     return plan
 
@@ -285,7 +291,10 @@ def cpu_sample(w: Workload, budget_s=20.0):
     return Ms * w.ntransf / dt, cores, sample
 
 
-def accuracy(w: Workload, out_first: np.ndarray, seed=3):
+def accuracy(w: Workload, out_first: np.ndarray, seed=3, oracle_same_width=True, ns=None):
+    """rel-l2 error of the first transform against FP64 direct sums on a
+    seeded subset of modes/targets, and (oracle_same_width) the oracle's own
+    error at kernel width ns on the same subset."""
     from oracle import oracle as O
     O.set_num_threads(os.cpu_count() or 1)
     pts = [p.astype(np.float64) for p in w.points()] + [None] * (3 - w.dim)
@@ -305,8 +314,8 @@ def accuracy(w: Workload, out_first: np.ndarray, seed=3):
     # width and shape for this tol) at the same modes/targets: the error the
     # reference's parameter rule itself leaves, beside ours
     oracle_err = None
-    if pts[0].size <= 4_000_000:
-        plan = oracle_plan(w, os.cpu_count() or 1)
+    if oracle_same_width and pts[0].size <= 4_000_000:
+        plan = oracle_plan(w, os.cpu_count() or 1, ns=ns)
         full = cpu_step(plan, w, [p for p in pts if p is not None], w.data().astype(np.complex128))
         o = np.asarray(full)[0].ravel()[idx]
         oracle_err = float(np.linalg.norm(o - ref) / np.linalg.norm(ref))
@@ -411,40 +420,19 @@ def _time_device(plan, args_ce, steps, stream, flush):
     return sum(a.elapsed_time(b) for a, b in ev)
 
 
-def run_ours(args, w: Workload, rank, world, local_rank):
+def _tuned_plan(w: Workload, dev, stream, opts, pts_dev, args_ce, flush, tuned: bool):
+    """The plan to time.  Tuned: the learned selector's layout (gpu_method 0)
+    against the library autotuner's best layout class on a second plan over
+    the same points; a few flushed executes of each decide which is kept.
+    Returns (plan, autotuner entry if it won else None, selector's plan info)."""
     import torch
-    dev = torch.device("cuda", local_rank)
-    torch.cuda.set_device(dev)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist  # noqa: F811
-    pts = w.points()
-    M = pts[0].size
-    data = w.data()
-    # tuned form: the library chooses the method (gpu_method 0) unless given
-    opts = {"gpu_method": args.method}
-    if args.kerevalmeth is not None:
-        opts["gpu_kerevalmeth"] = args.kerevalmeth
-    elif args.method == 0 and not w.single:
-        # tuned FP64: the fitted piecewise-polynomial kernel (Horner) instead
-        # of exp(beta sqrt(1 - c x^2)) in FP64 -- same error against the
-        # oracle, a third less interpolation time on GB300's FP64 units
-        opts["gpu_kerevalmeth"] = 1
-    stream = torch.cuda.Stream(device=dev)
     plan = _make_plan(w, dev, stream, opts)
-    pts_dev = [torch.from_numpy(p).to(dev) for p in pts]
-    data_dev = torch.from_numpy(data).to(dev)
-    inp, out, args_ce = _io_tensors(w, data_dev, M, dev)
     with torch.cuda.stream(stream):
         plan.set_pts(*pts_dev[::-1])  # the Python interface takes C-ordered axes
     torch.cuda.synchronize()
     selector_info = plan.info()
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     tune = None
-    if args.method == 0:
-        # tuned form: the learned selector's layout (gpu_method 0) against the
-        # library autotuner's best layout class on a second plan over the same
-        # points; a few flushed executes of each decide which is timed
+    if tuned:
         alt = _make_plan(w, dev, stream, opts)
         with torch.cuda.stream(stream):
             alt.set_pts(*pts_dev[::-1])
@@ -462,6 +450,43 @@ def run_ours(args, w: Workload, rank, world, local_rank):
                 plan, alt = alt, plan
                 tune = best
         del alt
+    return plan, tune, selector_info
+
+
+def _tuned_opts(args, w: Workload):
+    # tuned form: the library chooses the method (gpu_method 0) unless given
+    opts = {"gpu_method": args.method}
+    if args.kerevalmeth is not None:
+        opts["gpu_kerevalmeth"] = args.kerevalmeth
+    elif args.method == 0 and not w.single:
+        # tuned FP64: the fitted piecewise-polynomial kernel (Horner) instead
+        # of exp(beta sqrt(1 - c x^2)) in FP64 -- same error against the
+        # oracle, a third less interpolation time on GB300's FP64 units
+        opts["gpu_kerevalmeth"] = 1
+    return opts
+
+
+def run_ours(args, w: Workload, rank, world, local_rank, extra=False):
+    """Times the workload and returns its JSON line (rank 0; None on other
+    ranks).  `extra`: a second workload of the default run, device time only
+    (no e2e, clocks or CPU leg), returned as a smaller record."""
+    import torch
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+    pts = w.points()
+    M = pts[0].size
+    data = w.data()
+    opts = dict(_tuned_opts(args, w), width_rule=args.width_rule)
+    stream = torch.cuda.Stream(device=dev)
+    pts_dev = [torch.from_numpy(p).to(dev) for p in pts]
+    data_dev = torch.from_numpy(data).to(dev)
+    inp, out, args_ce = _io_tensors(w, data_dev, M, dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    plan, tune, selector_info = _tuned_plan(w, dev, stream, opts, pts_dev, args_ce, flush,
+                                            args.method == 0)
     with torch.cuda.stream(stream):
         plan.execute(*args_ce)
     torch.cuda.synchronize()
@@ -480,15 +505,16 @@ def run_ours(args, w: Workload, rank, world, local_rank):
 
     # ---- timed: device-resident inputs (each execute replays the plan's
     # CUDA graph of its launches)
-    clocks = ClockSampler(local_rank)
-    clocks.start()
+    clocks = None if extra else ClockSampler(local_rank)
+    if clocks:
+        clocks.start()
     barrier()
     torch.cuda.synchronize()
     t_start = time.time()
     dev_ms = _time_device(plan, args_ce, args.steps, stream, flush)
     t_end = time.time()
     barrier()
-    clk = clocks.stop(t_start, t_end)
+    clk = clocks.stop(t_start, t_end) if clocks else None
 
     # ---- stage times (roofline): the same executes with the library's stage
     # events on, which launches the kernels directly, over a second timed pass
@@ -499,10 +525,11 @@ def run_ours(args, w: Workload, rank, world, local_rank):
     stages = plan.stage_times(reset=True)
     plan.set_timing(False)
 
-    # ---- plain form: the reference's default options, same inputs
+    # ---- plain form: the reference's default options (method, bins, exp
+    # kernel) at the same kernel width, same inputs
     plain_ms = None
     if not args.no_plain:
-        plain = _make_plan(w, dev, stream, {})
+        plain = _make_plan(w, dev, stream, {"width_rule": args.width_rule})
         with torch.cuda.stream(stream):
             plain.set_pts(*pts_dev[::-1])
             for _ in range(args.warmup):
@@ -512,6 +539,55 @@ def run_ours(args, w: Workload, rank, world, local_rank):
         plain_ms = _time_device(plain, args_ce, plain_steps, stream, flush) / plain_steps
         plain_info = plain.info()
         del plain
+
+    # ---- parity form: the tuned form at the reference's own kernel width
+    # (its results are the reference algorithm's, parameter for parameter)
+    parity = None
+    if args.width_rule == "tol" and not args.no_plain:
+        ppl, ptune, _ = _tuned_plan(w, dev, stream, dict(opts, width_rule="reference"), pts_dev,
+                                    args_ce, flush, args.method == 0)
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                ppl.execute(*args_ce)
+        torch.cuda.synchronize()
+        par_out = out.cpu().numpy()
+        psteps = max(3, min(args.steps, 200))
+        par_ms = _time_device(ppl, args_ce, psteps, stream, flush) / psteps
+        pinfo = ppl.info()
+        parity = {"value": M * w.ntransf / (par_ms / 1e3), "ms_per_step": par_ms,
+                  "ns": pinfo["ns"], "method": pinfo["method"],
+                  "bins": [pinfo["binsizex"], pinfo["binsizey"], pinfo["binsizez"]][:w.dim],
+                  "note": "same tuned form at the reference's kernel width "
+                          "(ns = ceil(-log10(tol/10))), which leaves errors above tol"}
+        del ppl
+
+    if extra:
+        units = M * w.ntransf
+        err, nacc, _ = accuracy(w, out_first, oracle_same_width=False) if not args.no_accuracy \
+            else (None, 0, None)
+        perr = accuracy(w, par_out, oracle_same_width=False)[0] \
+            if (parity is not None and not args.no_accuracy) else None
+        if parity is not None:
+            parity["rel_l2_err"] = perr
+        return {"workload": w.desc, "value": units / (dev_ms / args.steps / 1e3),
+                "ms_per_step": dev_ms / args.steps, "steps": args.steps,
+                "dtype": "f32" if w.single else "f64", "ns": info["ns"],
+                "width_rule": args.width_rule, "method": info["method"],
+                "bins": [info["binsizex"], info["binsizey"], info["binsizez"]][:w.dim],
+                "cell_order": info["cell_order"], "kerevalmeth": info["kerevalmeth"],
+                "layout_from": None if args.method != 0 else (
+                    "autotuner" if tune is not None else "selector"),
+                "rel_l2_err": err, "rel_l2_points": nacc, "tol": w.tol,
+                "plain": None if plain_ms is None else {
+                    "value": units / (plain_ms / 1e3), "ms_per_step": plain_ms,
+                    "method": plain_info["method"],
+                    "note": "reference default options at the same kernel width"},
+                "parity_width": parity,
+                "stage_ms": {k: v / max(stages["batches"], 1) for k, v in stages.items()
+                             if k != "batches"},
+                "l2": "flushed between steps (256 MB write, outside the timed events)",
+                "timing": "device time of execute() (CUDA events on the plan stream), inputs "
+                          "resident"}
 
     # ---- e2e: host buffers through the public call; every step copies its
     # input from pinned host memory and its output back.  Two plans on two
@@ -587,7 +663,11 @@ def run_ours(args, w: Workload, rank, world, local_rank):
     units = M * w.ntransf
     value = replica_rate(world, units, args.steps, dev_ms)
     e2e_value = replica_rate(world, units, args.steps, e2e_ms)
-    err, nacc, oracle_err = accuracy(w, out_first) if not args.no_accuracy else (None, 0, None)
+    err, nacc, oracle_err = accuracy(w, out_first, ns=info["ns"]) if not args.no_accuracy \
+        else (None, 0, None)
+    if parity is not None:
+        parity["rel_l2_err"] = accuracy(w, par_out, oracle_same_width=False)[0] \
+            if not args.no_accuracy else None
 
     # roofline of the dominant kernel of ours: spread (type 1) / interp (type 2)
     s = 4 if w.single else 8
@@ -641,10 +721,13 @@ def run_ours(args, w: Workload, rank, world, local_rank):
                                 selector_info["binsizez"]][:w.dim]}},
         "rel_l2_err": err, "rel_l2_points": nacc, "tol": w.tol,
         "rel_l2_err_oracle_same_width": oracle_err,
+        "width_rule": args.width_rule,
+        "parity_width": parity,
         "plain": None if plain_ms is None else {
             "value": units / (plain_ms / 1e3), "ms_per_step": plain_ms,
-            "method": plain_info["method"],
-            "note": "reference default options (type 1: gpu_method 2, type 2: gpu_method 1)"},
+            "method": plain_info["method"], "ns": plain_info["ns"],
+            "note": "reference default options (type 1: gpu_method 2, type 2: gpu_method 1; "
+                    "bins, exp kernel) at the same kernel width"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(data.nbytes),
                 "d2h_bytes_per_step": int(out.numel() * out.element_size()),
                 "ms_per_step": e2e_ms / args.steps,
@@ -662,7 +745,7 @@ def run_ours(args, w: Workload, rank, world, local_rank):
         "clocks": clk,
         "wall_s_timed": t_end - t_start,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 class Batch64:
@@ -699,7 +782,9 @@ class Batch64:
                                "pts": [p.astype(np.float32) for p in pts], "c": c})
 
 
-def run_batch64(args, rank, world, local_rank):
+def run_batch64(args, rank, world, local_rank, extra=False):
+    """Config 4: tuned+batched against 64 plain plans; prints its JSON line
+    (returns it instead when `extra`)."""
     import torch
 
     from cufinufft_gb300 import cufinufft, cufinufft_batch
@@ -716,7 +801,8 @@ def run_batch64(args, rank, world, local_rank):
         plans, cs, fks, pts_keep = [], [], [], []
         for s in specs:
             p = cufinufft(1, s["modes"][::-1], n_trans=s["ntr"], eps=wl.tol, dtype=np.float32,
-                          maxbatchsize=s["ntr"] if whole_batch else 0, **opts)
+                          maxbatchsize=s["ntr"] if whole_batch else 0,
+                          width_rule=args.width_rule, **opts)
             p.set_stream(stream)
             pd = [torch.from_numpy(x).to(dev) for x in s["pts"]]
             with torch.cuda.stream(stream):
@@ -824,12 +910,13 @@ def run_batch64(args, rank, world, local_rank):
 
     for _ in range(args.warmup):
         run_batch()
-    clocks = ClockSampler(local_rank)
-    clocks.start()
+    clocks = None if extra else ClockSampler(local_rank)
+    if clocks:
+        clocks.start()
     t0 = time.time()
     batch_ms = timed(run_batch, args.steps)
     t1 = time.time()
-    clk = clocks.stop(t0, t1)
+    clk = clocks.stop(t0, t1) if clocks else None
     out_batch = [f.cpu().numpy() for f in fks2[:8]]
     agree = max(float(np.linalg.norm(a - b) / max(np.linalg.norm(a), 1e-30))
                 for a, b in zip(out_plain, out_batch))
@@ -843,7 +930,7 @@ def run_batch64(args, rank, world, local_rank):
         errs = []
         for s, fk in list(zip(specs, out_batch))[:8]:
             n = s["modes"][0] * s["modes"][1]
-            idx = rng.choice(n, size=16, replace=False)
+            idx = rng.choice(n, size=64, replace=False)
             ref = O.direct_type1(s["pts"][0].astype(np.float64), s["pts"][1].astype(np.float64),
                                  None, s["c"][0].astype(np.complex128), s["modes"], 1, idx)
             est = fk[0].ravel()[idx]
@@ -873,9 +960,12 @@ def run_batch64(args, rank, world, local_rank):
                      "per_plan_choice": {f"method {m} bins {b}" + (f" maxsub {c}" if c else ""): n
                                          for (m, b, c), n in chosen.items()}},
         "max_rel_diff_batched_vs_plain": agree,
-        "rel_l2_err": err, "tol": wl.tol,
+        "rel_l2_err": err, "tol": wl.tol, "width_rule": args.width_rule,
+        "rel_l2_note": "worst over the first 8 plans, 64 random modes each, vs FP64 direct sums",
         "clocks": clk,
     }
+    if extra:
+        return line
     print(json.dumps(line), flush=True)
 
 
@@ -892,6 +982,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the direct-sum check")
     ap.add_argument("--no-plain", action="store_true", help="skip the default-options plan")
+    ap.add_argument("--width-rule", choices=["tol", "reference"], default="tol",
+                    help="kernel width: 'tol' meets rel-l2 <= tol (the metric's gate), "
+                         "'reference' is the reference's ns = ceil(-log10(tol/10))")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload only: skip the 3D cluster and uneven-batch lines")
     args = ap.parse_args()
     if args.impl == "ours":
         args.warmup = max(args.warmup, 3)
@@ -916,7 +1011,23 @@ def main():
         torch.cuda.set_device(local_rank)
         dist.init_process_group("nccl")
     try:
-        run_ours(args, w, rank, world, local_rank)
+        line = run_ours(args, w, rank, world, local_rank)
+        if line is not None and world == 1 and args.workload == "radial2d" and not args.no_extras:
+            # the other headline configurations, device time only, in the same
+            # record: the 3D clustered type 1 and the uneven 64-plan batch
+            # (tuned+batched against plain plans)
+            import argparse as _ap
+            xa = _ap.Namespace(**vars(args))
+            xa.steps = max(3, min(args.steps, 10))
+            xa.warmup = 3
+            t0 = time.time()
+            extras = {"cluster3d": run_ours(xa, WORKLOADS["cluster3d"](), rank, world, local_rank,
+                                            extra=True),
+                      "batch64": run_batch64(xa, rank, world, local_rank, extra=True)}
+            extras["wall_s"] = time.time() - t0
+            line["extra_workloads"] = extras
+        if line is not None:
+            print(json.dumps(line), flush=True)
     finally:
         if world > 1:
             import torch.distributed as dist
