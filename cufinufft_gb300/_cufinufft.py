@@ -72,7 +72,8 @@ class PlanInfo(ctypes.Structure):
         "maxbatchsize", "method", "sort", "binsizex", "binsizey", "binsizez", "nbins",
         "nsubprob", "kerevalmeth")] + [("beta", c_double), ("es_c", c_double),
                                        ("line_fft", c_int), ("cell_order", c_int),
-                                       ("width_rule", c_int)]
+                                       ("width_rule", c_int), ("chain_fp32", c_int),
+                                       ("half_fft", c_int)]
 
 
 CufinufftPlan = c_void_p

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <new>
 #include <vector>
 
@@ -96,6 +97,25 @@ template <typename T> static void drop_graph(Plan<T>* p) {
 }
 
 template <typename T> static void release(Plan<T>* p) {
+  if (p->lo) {
+    release(p->lo);
+    delete p->lo;
+    p->lo = nullptr;
+  }
+  cudaFree(p->n_idx);
+  p->n_idx = nullptr;
+  for (int k = 0; k < 3; ++k) {
+    cudaFree(p->n_i0[k]);
+    cudaFree(p->n_d[k]);
+    p->n_i0[k] = nullptr;
+    p->n_d[k] = nullptr;
+  }
+  p->n_cap = 0;
+  cudaFree(p->c32);
+  p->c32 = nullptr;
+  p->c32_cap = 0;
+  cudaFree(p->fk32);
+  p->fk32 = nullptr;
   drop_graph(p);
   if (p->have_fft) cufftDestroy(p->fft);
   if (p->have_fft_rem) cufftDestroy(p->fft_rem);
@@ -112,6 +132,7 @@ template <typename T> static void release(Plan<T>* p) {
     p->rad[k].clear();
   }
   p->line_fft = false;
+  p->half_fft = false;
   p->horner.clear();
   cudaFree(p->sel_buf);
   p->sel_buf = nullptr;
@@ -190,6 +211,150 @@ static bool use_line_fft(const Plan<T>* p) {
     if (p->nf[k] > line_fft_cap<T>() || r.empty() || r.size() > 24) return false;
   }
   return true;
+}
+
+// Pruned power-of-two passes (halffft.cu): every axis nf = 2M with M a power
+// of two in [64, 1024] and at most M modes (always so at upsampfac 2).  The
+// default where they apply; CUFINUFFT_FFT=cufft (or line) selects another.
+template <typename T>
+static bool use_half_fft(const Plan<T>* p) {
+  const char* v = std::getenv("CUFINUFFT_FFT");
+  if (v && std::strcmp(v, "half") != 0) return false;
+  for (int k = 0; k < p->dim; ++k)
+    if (!half_fft_size_ok(p->nf[k]) || 2 * p->N[k] > p->nf[k]) return false;
+  return true;
+}
+
+// Twiddle tables W^m = exp(iflag 2 pi i m / nf_d), m < nf_d, per axis, in
+// extended precision on the host.
+template <typename T>
+static int make_twiddles(Plan<T>* p) {
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  for (int k = 0; k < p->dim; ++k) {
+    const int L = p->nf[k];
+    std::vector<cplx_t<T>> h((size_t)L);
+    for (int m = 0; m < L; ++m) {
+      const long double ang = two_pi * (long double)m / (long double)L;
+      h[m].x = (T)(double)cosl(ang);
+      h[m].y = (T)(double)((long double)p->iflag * sinl(ang));
+    }
+    CFG_CUDA(cudaMalloc(&p->tw[k], sizeof(cplx_t<T>) * (size_t)L));
+    CFG_CUDA(cudaMemcpy(p->tw[k], h.data(), sizeof(cplx_t<T>) * (size_t)L, cudaMemcpyHostToDevice));
+  }
+  return 0;
+}
+
+// The passes of one batch of B transforms (see halffft.cu): type 2 modes fk
+// -> x pass (amplification fused) -> y -> z -> grid fw2, intermediates in
+// fw; type 1 grid fw -> z -> y -> x pass (deconvolution fused) -> modes fk,
+// intermediates in fw2.
+template <typename T>
+static std::vector<HalfPass<T>> half_passes(const Plan<T>* p, cplx_t<T>* fk, int B) {
+  const long long L0 = p->nf[0], L1 = p->nf[1], L2 = p->nf[2];
+  const int N0 = p->N[0], N1 = p->N[1], N2 = p->N[2];
+  const long long Nm = (long long)N0 * N1 * N2, Nf = L0 * L1 * L2;
+  auto base = [&](int kind, int axis) {
+    HalfPass<T> a;
+    std::memset(&a, 0, sizeof(a));
+    a.kind = kind;
+    a.M = p->nf[axis] / 2;
+    a.N = p->N[axis];
+    a.tw = p->tw[axis];
+    a.ntr = B;
+    a.nouter = 1;
+    a.Na = 1;
+    return a;
+  };
+  auto cols_pitch = [](int n) { return ((n + 15) / 16) * 16 + 4; };  // 4 mod 16: conflict-free gathers
+  std::vector<HalfPass<T>> v;
+  if (p->type == 2) {
+    cplx_t<T>* t1 = p->fw;
+    cplx_t<T>* t2 = p->fw + (size_t)B * N2 * N1 * L0;
+    HalfPass<T> x = base(kHalfT2Rows, 0);
+    x.in = fk;
+    x.in_tr = Nm;
+    x.in_row = N0;
+    x.nlines = N1 * N2;
+    x.fac = p->fac[0];
+    x.fac_a = p->dim > 1 ? p->fac[1] : nullptr;
+    x.fac_b = p->dim > 2 ? p->fac[2] : nullptr;
+    x.Na = N1;
+    x.out = p->dim == 1 ? p->fw2 : t1;
+    x.out_tr = p->dim == 1 ? Nf : (long long)N2 * N1 * L0;
+    x.out_row = L0;
+    v.push_back(x);
+    if (p->dim >= 2) {
+      HalfPass<T> y = base(kHalfT2Cols, 1);
+      y.in = t1;
+      y.in_tr = (long long)N2 * N1 * L0;
+      y.in_row = L0;
+      y.in_plane = (long long)N1 * L0;
+      y.ncols = (int)L0;
+      y.nouter = p->dim == 3 ? N2 : 1;
+      y.out = p->dim == 2 ? p->fw2 : t2;
+      y.out_tr = p->dim == 2 ? Nf : (long long)N2 * L1 * L0;
+      y.out_row = L0;
+      y.out_plane = L1 * L0;
+      y.pitch = cols_pitch(N1);
+      v.push_back(y);
+    }
+    if (p->dim == 3) {
+      HalfPass<T> z = base(kHalfT2Cols, 2);
+      z.in = t2;
+      z.in_tr = (long long)N2 * L1 * L0;
+      z.in_row = L1 * L0;
+      z.ncols = (int)(L1 * L0);
+      z.out = p->fw2;
+      z.out_tr = Nf;
+      z.out_row = L1 * L0;
+      z.pitch = cols_pitch(N2);
+      v.push_back(z);
+    }
+    return v;
+  }
+  cplx_t<T>* s2 = p->fw2;
+  cplx_t<T>* s1 = p->dim == 3 ? p->fw2 + (size_t)B * N2 * L1 * L0 : p->fw2;
+  if (p->dim == 3) {
+    HalfPass<T> z = base(kHalfT1Cols, 2);
+    z.in = p->fw;
+    z.in_tr = Nf;
+    z.in_row = L1 * L0;
+    z.ncols = (int)(L1 * L0);
+    z.out = s2;
+    z.out_tr = (long long)N2 * L1 * L0;
+    z.out_row = L1 * L0;
+    z.pitch = cols_pitch((int)(L2 / 2));
+    v.push_back(z);
+  }
+  if (p->dim >= 2) {
+    HalfPass<T> y = base(kHalfT1Cols, 1);
+    y.in = p->dim == 3 ? s2 : p->fw;
+    y.in_tr = p->dim == 3 ? (long long)N2 * L1 * L0 : Nf;
+    y.in_row = L0;
+    y.in_plane = L1 * L0;
+    y.ncols = (int)L0;
+    y.nouter = p->dim == 3 ? N2 : 1;
+    y.out = s1;
+    y.out_tr = (long long)N2 * N1 * L0;
+    y.out_row = L0;
+    y.out_plane = (long long)N1 * L0;
+    y.pitch = cols_pitch((int)(L1 / 2));
+    v.push_back(y);
+  }
+  HalfPass<T> x = base(kHalfT1Rows, 0);
+  x.in = p->dim == 1 ? p->fw : s1;
+  x.in_tr = p->dim == 1 ? Nf : (long long)N2 * N1 * L0;
+  x.in_row = L0;
+  x.nlines = N1 * N2;
+  x.out = fk;
+  x.out_tr = Nm;
+  x.out_row = N0;
+  x.fac = p->fac[0];
+  x.fac_a = p->dim > 1 ? p->fac[1] : nullptr;
+  x.fac_b = p->dim > 2 ? p->fac[2] : nullptr;
+  x.Na = N1;
+  v.push_back(x);
+  return v;
 }
 
 template <typename T>
@@ -441,9 +606,12 @@ static int set_width_rule(int rule, int* previous) {
   return 0;
 }
 
+// sp_fixed: the kernel (width and shape) chosen by an FP64 plan for its FP32
+// chain, instead of this precision's rule.
 template <typename T>
 static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int iflag, int ntransf,
-                         double tol, int maxbatchsize, const cufinufft_opts* opts) {
+                         double tol, int maxbatchsize, const cufinufft_opts* opts,
+                         const SpreaderParams* sp_fixed = nullptr) {
   p->type = type;
   p->dim = dim;
   p->width_rule = width_rule_now();
@@ -456,6 +624,7 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   int ier = setup_spreader(tol, p->opts.upsampfac, p->opts.gpu_kerevalmeth, is_single<T>(), &p->sp,
                            p->width_rule, dim);
   if (ier > 1) return ier;
+  if (sp_fixed) p->sp = *sp_fixed;
   for (int k = 0; k < dim; ++k) p->N[k] = nmodes[k];
   setup_binsize(dim, &p->opts);
 
@@ -569,7 +738,14 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   for (int k = 0; k < dim; ++k) CFG_CUDA(cudaMalloc(&p->fac[k], sizeof(T) * (size_t)p->N[k]));
 
   int e = 0;
-  if (use_line_fft(p)) {
+  if (use_half_fft(p)) {
+    // pruned power-of-two passes: no cuFFT plan; type 2 grid in fw2
+    // (intermediates in fw), type 1 intermediates in fw2
+    e = make_twiddles(p);
+    if (e) return e;
+    CFG_CUDA(cudaMalloc(&p->fw2, sizeof(cplx_t<T>) * (size_t)Nf * p->maxbatch));
+    p->half_fft = true;
+  } else if (use_line_fft(p)) {
     e = make_line_fft(p);
     if (e) return e;
   } else {
@@ -717,8 +893,14 @@ static int bank_order(Plan<T>* p, int method, const int bs[3], int nbins, BankOr
 template <typename T>
 static int build_subproblems(Plan<T>* p);
 
+static int setpts_chain(Plan<double>* p, int M, const double* x, const double* y, const double* z);
+static int execute_chain(Plan<double>* p, double2* c, double2* fk);
+
 template <typename T>
 static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (p->lo) return setpts_chain(p, M, x, y, z);
+  }
   if (!p->planned) return CUFINUFFT_ERR_GENERIC;
   if (M < 0) return CUFINUFFT_ERR_ARG;
   const T* xs[3] = {x, y, z};
@@ -867,7 +1049,13 @@ static int execute_direct(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
       CFG_CUDA(cudaMemsetAsync(p->fw, 0, sizeof(cplx_t<T>) * (size_t)Nf * B, p->stream));
       CFG_CUDA(run_spread(p, a));
       mark(p, ev[1]);
-      if (p->line_fft) {
+      if (p->half_fft) {
+        const std::vector<HalfPass<T>> passes = half_passes(p, fk + (size_t)b0 * Nm, B);
+        for (size_t i = 0; i < passes.size(); ++i) {
+          if (i + 1 == passes.size()) mark(p, ev[2]);  // last pass: deconvolution fused
+          CFG_CUDA(launch_half_pass<T>(passes[i], p->stream));
+        }
+      } else if (p->line_fft) {
         const std::vector<LineArgs<T>> passes = line_passes(p, fk + (size_t)b0 * Nm, B);
         for (size_t i = 0; i < passes.size(); ++i) {
           if (i + 1 == passes.size()) mark(p, ev[2]);  // last pass: deconvolution fused
@@ -880,7 +1068,14 @@ static int execute_direct(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
                                       p->fac[1], p->fac[2], B, p->stream));
       }
     } else {
-      if (p->line_fft) {
+      if (p->half_fft) {
+        const std::vector<HalfPass<T>> passes = half_passes(p, fk + (size_t)b0 * Nm, B);
+        for (size_t i = 0; i < passes.size(); ++i) {
+          CFG_CUDA(launch_half_pass<T>(passes[i], p->stream));
+          if (i == 0) mark(p, ev[1]);  // first pass: amplification fused
+        }
+        mark(p, ev[2]);
+      } else if (p->line_fft) {
         const std::vector<LineArgs<T>> passes = line_passes(p, fk + (size_t)b0 * Nm, B);
         for (size_t i = 0; i < passes.size(); ++i) {
           CFG_CUDA(launch_line_fft<T>(passes[i], p->stream));
@@ -946,6 +1141,9 @@ static int take_status(Plan<T>* p) {
 
 template <typename T>
 static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (p->lo) return execute_chain(p, c, fk);
+  }
   if (const int e = take_status(p)) return e;
   if (p->timing || !p->planned || !graphs_enabled()) return execute_direct(p, c, fk);
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -981,14 +1179,228 @@ static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
   return execute_direct(p, c, fk);
 }
 
+// ---------------------------------------------------------------------------
+// The FP32 chain of FP64 plans.  An FP64 plan whose tolerance is at least
+// kChainTol makes an FP32 plan `lo` with the FP64 plan's kernel (width from
+// the FP64 rule, beta and c rounded to FP32, Fourier-series factors
+// evaluated in FP64 for that kernel) and runs spreading/interpolation, the
+// FFT and the deconvolution there.  The FP64 side keeps what needs FP64:
+// folding and rescaling the points (first tap and tap offset computed in
+// FP64, the offset in [0,1) then rounded to FP32) and the conversion of c
+// and fk.  On GB300, whose FP64 units are a small fraction of its FP32
+// throughput, this moves the FP64 plan to the FP32 plan's speed.  FP32
+// rounding of the chain leaves ~2-4e-7 relative l2 on large grids (an FP32
+// FFT of 256^2..2048^2 alone 1.5-1.8e-7), so the chain is taken from tol
+// 1e-6 up, where that stays below tol; CUFINUFFT_FP64_CHAIN=1 keeps every
+// FP64 plan in FP64 throughout, as the reference's FP64 build does.
+constexpr double kChainTol = 1e-6;
+
+static bool chain_wanted(int type, double tol, const cufinufft_opts* opts) {
+  if (type != 1 && type != 2) return false;
+  if (opts && opts->gpu_spreadinterponly) return false;
+  if (!(tol >= kChainTol)) return false;
+  const char* v = std::getenv("CUFINUFFT_FP64_CHAIN");
+  return !(v && v[0] == '1');
+}
+
+// The FP64 plan's view of its chain (what info, the batch and the layout
+// calls read).
+static void sync_from_lo(Plan<double>* p) {
+  const Plan<float>* q = p->lo;
+  for (int k = 0; k < 3; ++k) {
+    p->N[k] = q->N[k];
+    p->nf[k] = q->nf[k];
+    p->bs[k] = q->bs[k];
+    p->nb[k] = q->nb[k];
+  }
+  p->ntransf = q->ntransf;
+  p->maxbatch = q->maxbatch;
+  p->iflag = q->iflag;
+  p->rem = q->rem;
+  p->opts = q->opts;
+  p->method = q->method;
+  p->variant = q->variant;
+  p->auto_method = q->auto_method;
+  p->sort = q->sort;
+  p->nbins = q->nbins;
+  p->M = q->M;
+  p->nsub = q->nsub;
+  p->cell_order = q->cell_order;
+  p->line_fft = q->line_fft;
+  p->half_fft = q->half_fft;
+  p->spread_only = q->spread_only;
+  p->planned = q->planned;
+  p->pts_set = q->pts_set;
+  p->stream = q->stream;
+  p->timing = q->timing;
+}
+
+static int makeplan_chain(Plan<double>* p, int type, int dim, const int* nmodes, int iflag, int ntransf,
+                          double tol, int maxbatchsize, const cufinufft_opts* opts) {
+  p->type = type;
+  p->dim = dim;
+  p->width_rule = width_rule_now();
+  if (opts) p->opts = *opts;
+  else default_opts(type, dim, &p->opts);
+  int ier = setup_spreader(tol, p->opts.upsampfac, p->opts.gpu_kerevalmeth, false, &p->sp, p->width_rule,
+                           dim);
+  if (ier > 1) return ier;
+  SpreaderParams sp = p->sp;
+  sp.beta = (double)(float)sp.beta;  // the FP32 kernel's shape, exactly
+  sp.c = (double)(float)sp.c;
+  p->lo = new (std::nothrow) Plan<float>();
+  if (!p->lo) return CUFINUFFT_ERR_ALLOC;
+  p->lo->device = p->device;
+  ier = makeplan_impl<float>(p->lo, type, dim, nmodes, iflag, ntransf, tol, maxbatchsize, opts, &sp);
+  if (ier) return ier;
+  sync_from_lo(p);
+  const long long Nm = (long long)p->N[0] * p->N[1] * p->N[2];
+  CFG_CUDA(cudaMalloc(&p->fk32, sizeof(cplx_t<float>) * (size_t)(Nm * p->ntransf)));
+  return 0;
+}
+
+// Sort of points already placed (first taps and FP32 offsets in caller
+// order): the counting sort of setpts, fed from stored arrays instead of
+// coordinates (the rebin kernels).
+static int setpts_placed(Plan<float>* q, int M, const int* s_idx, int* const s_i0[3], float* const s_d[3]) {
+  if (!q->planned) return CUFINUFFT_ERR_GENERIC;
+  q->pts_set = false;
+  ++q->version;
+  int e = ensure_points(q, M);
+  if (e) return e;
+  q->M = M;
+  q->nsub = 0;
+  if (M > 0 && q->method == 1 && q->sort == 0) {
+    CFG_CUDA(cudaMemcpyAsync(q->idx, s_idx, sizeof(int) * (size_t)M, cudaMemcpyDeviceToDevice, q->stream));
+    for (int k = 0; k < q->dim; ++k) {
+      CFG_CUDA(cudaMemcpyAsync(q->i0[k], s_i0[k], sizeof(int) * (size_t)M, cudaMemcpyDeviceToDevice,
+                               q->stream));
+      CFG_CUDA(cudaMemcpyAsync(q->d[k], s_d[k], sizeof(float) * (size_t)M, cudaMemcpyDeviceToDevice,
+                               q->stream));
+    }
+  } else if (!(q->method == 1 && q->sort == 0)) {
+    RebinArgs<float> a;
+    std::memset(&a, 0, sizeof(a));
+    a.dim = q->dim;
+    a.M = M;
+    for (int k = 0; k < 3; ++k) {
+      a.bs[k] = q->bs[k];
+      a.nb[k] = q->nb[k];
+      a.src_i0[k] = k < q->dim ? s_i0[k] : nullptr;
+      a.src_d[k] = k < q->dim ? s_d[k] : nullptr;
+      a.i0[k] = q->i0[k];
+      a.d[k] = q->d[k];
+    }
+    a.src_idx = s_idx;
+    a.idx = q->idx;
+    a.count = q->count;
+    a.rank = q->rank;
+    a.start = q->start;
+    CFG_CUDA(cudaMemsetAsync(q->count, 0, sizeof(int) * (size_t)q->nbins, q->stream));
+    e = bank_order(q, q->method, q->bs, q->nbins, &a.bank, q->cell_order);
+    if (e) return e;
+    CFG_CUDA(launch_rebin_count<float>(a, q->stream));
+    CFG_CUDA(launch_scan(q->count, q->start, q->nbins, 0, 1, q->scan_tmp, q->stream));
+    if (a.bank.cell_order)
+      CFG_CUDA(launch_scan(q->cls_count, q->cls_start, q->nbins * a.bank.ncls, 2, dense_run(q->dim),
+                           q->cls_tmp, q->stream));
+    CFG_CUDA(launch_rebin_permute<float>(a, q->stream));
+    if (q->method == 2) {
+      e = build_subproblems(q);
+      if (e) return e;
+    }
+  }
+  CFG_CUDA(cudaGetLastError());
+  q->pts_set = true;
+  return select_layout(q);
+}
+
+static int setpts_chain(Plan<double>* p, int M, const double* x, const double* y, const double* z) {
+  Plan<float>* q = p->lo;
+  if (!q->planned) return CUFINUFFT_ERR_GENERIC;
+  if (M < 0) return CUFINUFFT_ERR_ARG;
+  const double* xs[3] = {x, y, z};
+  for (int k = 0; k < p->dim; ++k)
+    if (M > 0 && xs[k] == nullptr) return CUFINUFFT_ERR_ARG;
+  ++p->version;
+  p->pts_set = q->pts_set = false;
+  if ((size_t)M > p->n_cap || p->n_idx == nullptr) {
+    cudaFree(p->n_idx);
+    p->n_idx = nullptr;
+    for (int k = 0; k < 3; ++k) {
+      cudaFree(p->n_i0[k]);
+      cudaFree(p->n_d[k]);
+      p->n_i0[k] = nullptr;
+      p->n_d[k] = nullptr;
+    }
+    cudaFree(p->c32);
+    p->c32 = nullptr;
+    p->n_cap = p->c32_cap = 0;
+    const size_t n = (size_t)std::max(M, 1);
+    CFG_CUDA(cudaMalloc(&p->n_idx, sizeof(int) * n));
+    for (int k = 0; k < p->dim; ++k) {
+      CFG_CUDA(cudaMalloc(&p->n_i0[k], sizeof(int) * n));
+      CFG_CUDA(cudaMalloc(&p->n_d[k], sizeof(float) * n));
+    }
+    CFG_CUDA(cudaMalloc(&p->c32, sizeof(cplx_t<float>) * n * (size_t)p->ntransf));
+    p->n_cap = n;
+    p->c32_cap = n * (size_t)p->ntransf;
+  }
+  NarrowPlaceArgs na;
+  std::memset(&na, 0, sizeof(na));
+  for (int k = 0; k < 3; ++k) {
+    na.x[k] = k < p->dim ? xs[k] : nullptr;
+    na.ax[k] = axis_map<double>(q->nf[k], q->sp.ns);
+    na.i0[k] = p->n_i0[k];
+    na.d[k] = p->n_d[k];
+  }
+  na.dim = p->dim;
+  na.M = M;
+  na.idx = p->n_idx;
+  CFG_CUDA(launch_place_narrow(na, q->stream));
+  const int e = setpts_placed(q, M, p->n_idx, p->n_i0, p->n_d);
+  sync_from_lo(p);
+  return e;
+}
+
+static int execute_chain(Plan<double>* p, double2* c, double2* fk) {
+  Plan<float>* q = p->lo;
+  if (!q->planned || !q->pts_set) return CUFINUFFT_ERR_GENERIC;
+  if (q->M > 0 && c == nullptr) return CUFINUFFT_ERR_ARG;
+  if (fk == nullptr) return CUFINUFFT_ERR_ARG;
+  const long long nc = (long long)q->ntransf * q->M;
+  const long long nk = (long long)q->ntransf * q->N[0] * q->N[1] * q->N[2];
+  int e = 0;
+  if (q->type == 1) {
+    CFG_CUDA(launch_narrow_complex(c, p->c32, nc, q->stream));
+    e = execute_impl(q, p->c32, p->fk32);
+    if (e) return e;
+    CFG_CUDA(launch_widen_complex(p->fk32, fk, nk, q->stream));
+  } else {
+    CFG_CUDA(launch_narrow_complex(fk, p->fk32, nk, q->stream));
+    e = execute_impl(q, p->c32, p->fk32);
+    if (e) return e;
+    CFG_CUDA(launch_widen_complex(p->c32, c, nc, q->stream));
+  }
+  return 0;
+}
+
 // Entry points for the batch (batch.cu): a plan's whole execute, and moving
 // a plan's work, cuFFT plans included, to another stream.
 template <typename T>
 int execute_plan(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (p->lo) return execute_chain(p, c, fk);
+  }
   return execute_direct(p, c, fk);
 }
 template <typename T>
 int plan_use_stream(Plan<T>* p, cudaStream_t s) {
+  if (p->lo) {
+    const int e = plan_use_stream(p->lo, s);
+    p->stream = s;
+    return e;
+  }
   p->stream = s;
   if (p->have_fft) CFG_CUFFT(cufftSetStream(p->fft, s));
   if (p->have_fft_rem) CFG_CUFFT(cufftSetStream(p->fft_rem, s));
@@ -1025,6 +1437,7 @@ static void fill_info(const Plan<T>* p, cufinufft_plan_info* info) {
   info->beta = p->sp.beta;
   info->es_c = p->sp.c;
   info->line_fft = p->line_fft ? 1 : 0;
+  info->half_fft = p->half_fft ? 1 : 0;
   info->cell_order = p->cell_order ? 1 : 0;
   info->width_rule = p->width_rule;
 }
@@ -1470,7 +1883,15 @@ static int makeplan_entry(int type, int dim, int* nmodes, int iflag, int ntransf
   }
   DeviceGuard g(p->device);
   if (!g.ok) return CUFINUFFT_ERR_CUDA;
-  int ier = makeplan_impl<T>(p, type, dim, nmodes, iflag, ntransf, tol, maxbatchsize, opts);
+  int ier;
+  if constexpr (std::is_same<T, double>::value) {
+    if (chain_wanted(type, tol, opts)) {
+      ier = makeplan_chain(p, type, dim, nmodes, iflag, ntransf, tol, maxbatchsize, opts);
+      if (ier) release(p);
+      return ier;
+    }
+  }
+  ier = makeplan_impl<T>(p, type, dim, nmodes, iflag, ntransf, tol, maxbatchsize, opts);
   if (ier) release(p);
   return ier;
 }
@@ -1508,21 +1929,35 @@ static int destroy_entry(H* h) {
   return 0;
 }
 
+// The plan that does the work: an FP64 plan's FP32 chain when it has one.
+static cfg::Plan<float>* chain_of(cufinufft_plan h) { return h->p.lo; }
+static cfg::Plan<float>* chain_of(cufinufftf_plan) { return nullptr; }
+static void after_chain_call(cufinufft_plan h) {
+  if (h->p.lo) cfg::sync_from_lo(&h->p);
+}
+static void after_chain_call(cufinufftf_plan) {}
+
+template <typename P>
+static int stage_times_impl(P* p, double* ms, long long* batches, int reset) {
+  int e = cfg::collect_times(p);
+  if (e) return e;
+  e = cfg::take_status(p);
+  if (e) return e;
+  for (int k = 0; k < 3; ++k) ms[k] = p->stage_ms[k];
+  if (batches) *batches = p->stage_batches;
+  if (reset) {
+    for (int k = 0; k < 3; ++k) p->stage_ms[k] = 0;
+    p->stage_batches = 0;
+  }
+  return 0;
+}
+
 template <typename H>
 static int stage_times_entry(H* h, double* ms, long long* batches, int reset) {
   if (!h || !ms) return CUFINUFFT_ERR_GENERIC;
   DeviceGuard g(h->p.device);
-  int e = cfg::collect_times(&h->p);
-  if (e) return e;
-  e = cfg::take_status(&h->p);
-  if (e) return e;
-  for (int k = 0; k < 3; ++k) ms[k] = h->p.stage_ms[k];
-  if (batches) *batches = h->p.stage_batches;
-  if (reset) {
-    for (int k = 0; k < 3; ++k) h->p.stage_ms[k] = 0;
-    h->p.stage_batches = 0;
-  }
-  return 0;
+  if (cfg::Plan<float>* q = chain_of(h)) return stage_times_impl(q, ms, batches, reset);
+  return stage_times_impl(&h->p, ms, batches, reset);
 }
 
 template <typename H>
@@ -1530,13 +1965,50 @@ static int set_layout_entry(H* h, int method, int bx, int by, int bz, int maxsub
   if (!h) return CUFINUFFT_ERR_GENERIC;
   DeviceGuard g(h->p.device);
   int bs[3] = {bx, by, bz};
+  if (cfg::Plan<float>* q = chain_of(h)) {
+    ++h->p.version;
+    const int e = cfg::set_layout_impl(q, method, bs, maxsub);
+    after_chain_call(h);
+    return e;
+  }
   return cfg::set_layout_impl(&h->p, method, bs, maxsub);
 }
 template <typename H>
 static int autotune_entry(H* h, cufinufft_tune_entry* out, int max_out, int* n_out) {
   if (!h) return CUFINUFFT_ERR_GENERIC;
   DeviceGuard g(h->p.device);
+  if (cfg::Plan<float>* q = chain_of(h)) {
+    ++h->p.version;
+    const int e = cfg::autotune_impl(q, out, max_out, n_out);
+    after_chain_call(h);
+    return e;
+  }
   return cfg::autotune_impl(&h->p, out, max_out, n_out);
+}
+
+template <typename H>
+static int set_stream_entry(H* h, cudaStream_t stream) {
+  if (!h || !h->p.planned) return CUFINUFFT_ERR_GENERIC;
+  auto set = [stream](auto* p) {
+    p->stream = stream ? stream : p->own;
+    if (p->have_fft && cufftSetStream(p->fft, p->stream) != CUFFT_SUCCESS) return CUFINUFFT_ERR_CUFFT;
+    if (p->have_fft_rem && cufftSetStream(p->fft_rem, p->stream) != CUFFT_SUCCESS) return CUFINUFFT_ERR_CUFFT;
+    return 0;
+  };
+  if (cfg::Plan<float>* q = chain_of(h)) {
+    const int e = set(q);
+    after_chain_call(h);
+    return e;
+  }
+  return set(&h->p);
+}
+
+template <typename H>
+static int set_timing_entry(H* h, int on) {
+  if (!h) return CUFINUFFT_ERR_GENERIC;
+  h->p.timing = on != 0;
+  if (cfg::Plan<float>* q = chain_of(h)) q->timing = on != 0;
+  return 0;
 }
 
 extern "C" {
@@ -1581,32 +2053,14 @@ int cufinufft_destroy(cufinufft_plan plan) { return destroy_entry(plan); }
 int cufinufftf_destroy(cufinufftf_plan plan) { return destroy_entry(plan); }
 
 int cufinufft_set_stream(cufinufft_plan plan, cudaStream_t stream) {
-  if (!plan || !plan->p.planned) return CUFINUFFT_ERR_GENERIC;
-  plan->p.stream = stream ? stream : plan->p.own;
-  if (plan->p.have_fft && cufftSetStream(plan->p.fft, plan->p.stream) != CUFFT_SUCCESS) return CUFINUFFT_ERR_CUFFT;
-  if (plan->p.have_fft_rem && cufftSetStream(plan->p.fft_rem, plan->p.stream) != CUFFT_SUCCESS)
-    return CUFINUFFT_ERR_CUFFT;
-  return 0;
+  return set_stream_entry(plan, stream);
 }
 int cufinufftf_set_stream(cufinufftf_plan plan, cudaStream_t stream) {
-  if (!plan || !plan->p.planned) return CUFINUFFT_ERR_GENERIC;
-  plan->p.stream = stream ? stream : plan->p.own;
-  if (plan->p.have_fft && cufftSetStream(plan->p.fft, plan->p.stream) != CUFFT_SUCCESS) return CUFINUFFT_ERR_CUFFT;
-  if (plan->p.have_fft_rem && cufftSetStream(plan->p.fft_rem, plan->p.stream) != CUFFT_SUCCESS)
-    return CUFINUFFT_ERR_CUFFT;
-  return 0;
+  return set_stream_entry(plan, stream);
 }
 
-int cufinufft_set_timing(cufinufft_plan plan, int on) {
-  if (!plan) return CUFINUFFT_ERR_GENERIC;
-  plan->p.timing = on != 0;
-  return 0;
-}
-int cufinufftf_set_timing(cufinufftf_plan plan, int on) {
-  if (!plan) return CUFINUFFT_ERR_GENERIC;
-  plan->p.timing = on != 0;
-  return 0;
-}
+int cufinufft_set_timing(cufinufft_plan plan, int on) { return set_timing_entry(plan, on); }
+int cufinufftf_set_timing(cufinufftf_plan plan, int on) { return set_timing_entry(plan, on); }
 
 int cufinufft_stage_times(cufinufft_plan plan, double* ms, long long* batches, int reset) {
   return stage_times_entry(plan, ms, batches, reset);
@@ -1631,6 +2085,7 @@ int cufinufftf_autotune(cufinufftf_plan plan, cufinufft_tune_entry* out, int max
 int cufinufft_features(cufinufft_plan plan, float* features) {
   if (!plan || !features) return CUFINUFFT_ERR_GENERIC;
   DeviceGuard g(plan->p.device);
+  if (plan->p.lo) return cfg::features_impl(plan->p.lo, features);
   return cfg::features_impl(&plan->p, features);
 }
 int cufinufftf_features(cufinufftf_plan plan, float* features) {
@@ -1641,6 +2096,12 @@ int cufinufftf_features(cufinufftf_plan plan, float* features) {
 int cufinufft_set_layout_class(cufinufft_plan plan, int cls) {
   if (!plan) return CUFINUFFT_ERR_GENERIC;
   DeviceGuard g(plan->p.device);
+  if (plan->p.lo) {
+    ++plan->p.version;
+    const int e = cfg::apply_layout_class(plan->p.lo, cls);
+    cfg::sync_from_lo(&plan->p);
+    return e;
+  }
   return cfg::apply_layout_class(&plan->p, cls);
 }
 int cufinufftf_set_layout_class(cufinufftf_plan plan, int cls) {
@@ -1653,6 +2114,13 @@ int cufinufft_set_width_rule(int rule, int* previous) { return cfg::set_width_ru
 
 int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info) {
   if (!plan || !info) return CUFINUFFT_ERR_GENERIC;
+  if (plan->p.lo) {
+    cfg::fill_info(plan->p.lo, info);
+    info->beta = plan->p.sp.beta;  // the FP64 plan's kernel (the chain's is beta, c rounded to FP32)
+    info->es_c = plan->p.sp.c;
+    info->chain_fp32 = 1;
+    return 0;
+  }
   cfg::fill_info(&plan->p, info);
   return 0;
 }

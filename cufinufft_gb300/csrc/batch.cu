@@ -237,6 +237,8 @@ static int batch_make(Batch<T>* b, int nplans, Plan<T>** plans) {
   const char* mode = std::getenv("CUFINUFFT_BATCH");
   b->by_plans = !(mode && std::strcmp(mode, "tables") == 0);
   if (b->by_plans) return 0;
+  for (Plan<T>* p : b->plans)
+    if (p->lo) return CUFINUFFT_ERR_ARG;  // the tables hold FP64 grids; an FP32 chain has none
   CFG_CUDA(cudaMallocHost(&b->h_desc, sizeof(BatchDesc<T>) * nplans));
   CFG_CUDA(cudaMalloc(&b->d_desc, sizeof(BatchDesc<T>) * nplans));
   long long task = 0, row = 0, blk = 0;

@@ -187,6 +187,38 @@ cudaError_t launch_amplify_modes(int dim, const int nf[3], const int N[3], cplx_
   return launch_mode_rows<T, true>(dim, nf, N, fk, fw, fac0, fac1, fac2, ntr, s);
 }
 
+// FP64 <-> FP32 complex conversion (the FP32 chain of an FP64 plan): one
+// 16-byte load and one 8-byte store per value, grid-stride.
+__global__ void k_narrow_complex(const double2* __restrict__ in, float2* __restrict__ out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double2 v = in[i];
+    out[i] = make_float2((float)v.x, (float)v.y);
+  }
+}
+__global__ void k_widen_complex(const float2* __restrict__ in, double2* __restrict__ out, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float2 v = in[i];
+    out[i] = make_double2((double)v.x, (double)v.y);
+  }
+}
+static int convert_grid(long long n) {
+  long long b = (n + 255) / 256;
+  if (b > 152LL * 16) b = 152LL * 16;
+  return b < 1 ? 1 : (int)b;
+}
+cudaError_t launch_narrow_complex(const double2* in, float2* out, long long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_narrow_complex<<<convert_grid(n), 256, 0, s>>>(in, out, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_widen_complex(const float2* in, double2* out, long long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_widen_complex<<<convert_grid(n), 256, 0, s>>>(in, out, n);
+  return cudaGetLastError();
+}
+
 template cudaError_t launch_amplify_modes<float>(int, const int*, const int*, cplx_t<float>*,
                                                  const cplx_t<float>*, const float*, const float*,
                                                  const float*, int, cudaStream_t);

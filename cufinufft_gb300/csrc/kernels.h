@@ -62,6 +62,23 @@ template <typename T> cudaError_t launch_bin_count(const PlaceArgs<T>& a, cudaSt
 template <typename T> cudaError_t launch_permute(const PlaceArgs<T>& a, cudaStream_t s);
 template <typename T> cudaError_t launch_place_unsorted(const PlaceArgs<T>& a, cudaStream_t s);
 
+// FP64 coordinates placed in FP64 (fold, rescale, first tap) with the tap
+// offset in [0,1) rounded to FP32, in caller order (idx[i] = i): the input
+// of an FP32 chain's sort in an FP64 plan.
+struct NarrowPlaceArgs {
+  const double* x[3];
+  AxisMap<double> ax[3];
+  int dim, M;
+  int* idx;
+  int* i0[3];
+  float* d[3];
+};
+cudaError_t launch_place_narrow(const NarrowPlaceArgs& a, cudaStream_t s);
+
+// Complex FP64 <-> FP32 conversion of n values.
+cudaError_t launch_narrow_complex(const double2* in, float2* out, long long n, cudaStream_t s);
+cudaError_t launch_widen_complex(const float2* in, double2* out, long long n, cudaStream_t s);
+
 // Re-binning of already placed points (no caller coordinates needed): the
 // bin of a point depends only on its first taps i0, so a new bin layout is a
 // counting sort of the stored arrays into fresh ones.
@@ -174,6 +191,36 @@ struct LineArgs {
   const T* fp;
   int fac_on_out;
 };
+
+// Pruned power-of-two passes (halffft.cu) for grids nf = 2M, M = 32 Q with
+// Q in {2, 4, 8, 16, 32}: per axis two M-point FFTs (one per output or input
+// parity) over the lines that hold modes.
+enum HalfKind { kHalfT2Rows = 0, kHalfT2Cols = 1, kHalfT1Cols = 2, kHalfT1Rows = 3 };
+template <typename T>
+struct HalfPass {
+  int kind;
+  int M, N;                   // FFT size (the axis has 2M grid points) and modes on this axis
+  const cplx_t<T>* in;
+  cplx_t<T>* out;
+  const cplx_t<T>* tw;        // W^t = exp(dir 2 pi i t / 2M), t < 2M
+  int ntr;                    // transforms; transform t at in + t in_tr, out + t out_tr
+  long long in_tr, out_tr;
+  // rows passes: nlines contiguous lines, line g at in + g in_row / out + g out_row;
+  // cols passes: in_row / out_row are the strides along the axis
+  int nlines;
+  long long in_row, out_row;
+  const T* fac;               // rows passes: factor of mode i along this axis (or null)
+  const T* fac_a;             // line factor fac_a[g % Na] * fac_b[g / Na] (or null)
+  const T* fac_b;
+  int Na;
+  // cols passes: ncols adjacent columns (a multiple of 4) x nouter lines,
+  // outer index o at in + o in_plane / out + o out_plane
+  int ncols, nouter;
+  long long in_plane, out_plane;
+  int pitch;                  // shared-memory pitch of a column (elements)
+};
+template <typename T> cudaError_t launch_half_pass(const HalfPass<T>& a, cudaStream_t s);
+bool half_fft_size_ok(int nf);
 
 template <typename T> int line_fft_cap();
 template <typename T> int line_fft_p2_elems();

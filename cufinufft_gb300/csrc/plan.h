@@ -42,6 +42,7 @@ template <typename T> struct Plan {
   // pruned line FFTs (fftpass.cu) instead of cuFFT: per-axis twiddle tables
   // exp(iflag 2 pi i m / nf_d) and radix sequences
   bool line_fft = false;
+  bool half_fft = false;  // pruned power-of-two passes (halffft.cu), tables in tw
   C* tw[3] = {nullptr, nullptr, nullptr};
   std::vector<int> rad[3];
   int rem = 0;
@@ -73,6 +74,18 @@ template <typename T> struct Plan {
   size_t cap_sparse = 0;
   unsigned char* sub_dense = nullptr;  // per subproblem: starts on a dense cell (cell order)
   size_t cap_sub_dense = 0;
+  // FP64 plans whose tolerance allows it run the spread/interp, FFT and
+  // deconvolution chain in FP32: `lo` is that FP32 plan (null otherwise).
+  // This side folds and rescales the points in FP64 (n_* arrays: caller
+  // order, input of lo's sort) and converts c / fk (c32, fk32).
+  Plan<float>* lo = nullptr;
+  int* n_idx = nullptr;
+  int* n_i0[3] = {nullptr, nullptr, nullptr};
+  float* n_d[3] = {nullptr, nullptr, nullptr};
+  size_t n_cap = 0;
+  cplx_t<float>* c32 = nullptr;
+  size_t c32_cap = 0;
+  cplx_t<float>* fk32 = nullptr;
   int* h_total = nullptr;  // pinned readback of the subproblem count
   // interpolation tile-wait status (SpreadArgs::status): host-mapped, two ints
   int* h_status = nullptr;

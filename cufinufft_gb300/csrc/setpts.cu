@@ -165,6 +165,21 @@ __global__ void __launch_bounds__(kPlaceThreads) k_place_unsorted(PlaceArgs<T> a
   }
 }
 
+__global__ void __launch_bounds__(kPlaceThreads) k_place_narrow(NarrowPlaceArgs a) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.M; i += gridDim.x * blockDim.x) {
+    a.idx[i] = i;
+    for (int k = 0; k < 3; ++k) {
+      if (k < a.dim) {
+        int i0;
+        double d;
+        place_coord<double>(a.x[k][i], a.ax[k], i0, d);
+        a.i0[k][i] = i0;
+        a.d[k][i] = (float)d;
+      }
+    }
+  }
+}
+
 static int place_grid(int M) {
   long long b = ((long long)M + kPlaceThreads - 1) / kPlaceThreads;
   if (b > 152LL * 64) b = 152LL * 64;
@@ -184,6 +199,12 @@ template <typename T> cudaError_t launch_permute(const PlaceArgs<T>& a, cudaStre
 template <typename T> cudaError_t launch_place_unsorted(const PlaceArgs<T>& a, cudaStream_t s) {
   if (a.M == 0) return cudaSuccess;
   k_place_unsorted<T><<<place_grid(a.M), kPlaceThreads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_place_narrow(const NarrowPlaceArgs& a, cudaStream_t s) {
+  if (a.M == 0) return cudaSuccess;
+  k_place_narrow<<<place_grid(a.M), kPlaceThreads, 0, s>>>(a);
   return cudaGetLastError();
 }
 

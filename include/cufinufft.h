@@ -110,6 +110,8 @@ typedef struct cufinufft_plan_info {
   int line_fft;   /* 1: pruned line FFTs (fftpass.cu), 0: cuFFT over the whole grid */
   int cell_order; /* 1: method 2 spreading over cell-ordered points (cell-run kernel) */
   int width_rule; /* kernel-width rule the plan was made under (cufinufft_set_width_rule) */
+  int chain_fp32; /* 1: an FP64 plan running its spread/interp, FFT and deconvolution in FP32 */
+  int half_fft;   /* 1: pruned power-of-two FFT passes (halffft.cu) instead of cuFFT */
 } cufinufft_plan_info;
 int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info);
 int cufinufftf_get_info(cufinufftf_plan plan, cufinufft_plan_info* info);

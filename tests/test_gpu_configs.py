@@ -104,17 +104,46 @@ def test_radial2d_type2_fp64(kerevalmeth):
            gpu_kerevalmeth=kerevalmeth)
 
 
-@pytest.mark.parametrize("rule,bound", [("reference", 3.0), ("tol", 1.0)])
-def test_cluster3d_type1_fp32(rule, bound):
+def test_cluster3d_type1_fp32_reference_width():
     rng = np.random.default_rng(9)
     M = 2_000_000
     pts = clustered3d(M)
     c = NC.strengths(rng, M)
-    err, info = _check(1, (128, 128, 128), pts, c, 1e-6, True, 1000, rule, bound * 1e-6,
+    err, info = _check(1, (128, 128, 128), pts, c, 1e-6, True, 1000, "reference", 3e-6,
                        gpu_method=0)
-    if rule == "reference":
-        # the learned selector sends these points to the cell-run layout
-        assert info["cell_order"] == 1, info
+    # the learned selector sends these points to the cell-run layout
+    assert info["cell_order"] == 1, info
+
+
+@pytest.mark.parametrize("layout", [(5, (16, 16, 2), 1024), (2, (16, 16, 2), 1024),
+                                    (1, (16, 16, 2), 1024)])
+def test_cluster3d_type1_fp32_tol_width(layout):
+    """At the tolerance-meeting width the kernel's own error is ~2e-7, and the
+    rest is FP32 accumulation: a million clustered points add into a few
+    hundred cells.  The cell-run layout sums each run in registers and meets
+    1e-6; layouts that add every point with FP32 atomics (shared tiles, or the
+    grid in L2) reach the FP32 accumulation floor of ~2e-6 on this input."""
+    import torch
+
+    from cufinufft_gb300 import cufinufft
+    rng = np.random.default_rng(9)
+    M = 2_000_000
+    modes = (128, 128, 128)
+    pts = [p.astype(np.float32) for p in clustered3d(M)]
+    c = NC.strengths(rng, M).astype(np.complex64)
+    plan = cufinufft(1, modes[::-1], eps=1e-6, dtype=np.float32, width_rule="tol")
+    plan.set_pts(*[torch.from_numpy(p).cuda() for p in pts[::-1]])
+    plan.set_layout(*layout)
+    fk = torch.zeros(modes[::-1], dtype=torch.complex64, device="cuda")
+    plan.execute(torch.from_numpy(c).cuda(), fk)
+    torch.cuda.synchronize()
+    out = fk.cpu().numpy().ravel()
+    idx = np.random.default_rng(3).choice(out.size, size=1000, replace=False)
+    p64 = [p.astype(np.float64) for p in pts]
+    d = NC.direct(1, modes, p64, c.astype(np.complex128), 1, idx)
+    err = np.linalg.norm(out[idx] - d) / np.linalg.norm(d)
+    bound = 1e-6 if layout[0] == 5 else 3e-6
+    assert err <= bound, (layout, err)
 
 
 def test_cluster3d_type2_fp64():

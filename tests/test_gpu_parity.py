@@ -52,7 +52,9 @@ def _case(ntype, dim, method, sort, single, kerevalmeth, tol, M=1500, ntr=1, max
                            **extra)
     ref = NC.oracle_nufft(ntype, modes, [p.astype(np.float64) for p in pts],
                           data.astype(np.complex128), tol, single, ntr=ntr, gpu_method=method)
-    same, dbound = _bounds(single, tol, kerevalmeth)
+    # an FP64 plan at tol >= 1e-6 runs its chain in FP32 (plan info
+    # chain_fp32): FP32 rounding bounds then
+    same, dbound = _bounds(single or info.get("chain_fp32", 0) == 1, tol, kerevalmeth)
     if edges:
         # a point exactly on a fold boundary (x = -pi, pi, -3pi) sits where
         # the kernel is cut off at |x| = ns/2; position roundings ~1e-16 of
