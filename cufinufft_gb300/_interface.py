@@ -75,8 +75,10 @@ def _size(a) -> int:
 class cufinufft:
     """A type-1 or type-2 NUFFT plan on one GPU.
 
-    :param nufft_type: 1 or 2 (3 raises, as in the reference).
-    :param modes: C-ordered shape of the mode array, 1 to 3 dimensions.
+    :param nufft_type: 1, 2 or 3 (type 3: nonuniform points to nonuniform
+        frequencies, which the reference reserves without implementing).
+    :param modes: C-ordered shape of the mode array, 1 to 3 dimensions (for
+        type 3 only its length, the dimension, is used).
     :param n_trans: number of transforms per execute.
     :param eps: requested relative tolerance.
     :param isign: sign of the exponent; default +1 for type 1, -1 for type 2.
@@ -162,8 +164,10 @@ class cufinufft:
         if ier != 0:
             raise RuntimeError('Error creating plan.')
 
-    def set_pts(self, kx, ky=None, kz=None):
-        """Set the nonuniform points (device arrays of the plan's real dtype)."""
+    def set_pts(self, kx, ky=None, kz=None, s=None, t=None, u=None):
+        """Set the nonuniform points (device arrays of the plan's real dtype);
+        type 3 also takes its target frequencies s (t, u in 2D/3D), in the
+        same C-ordered axis convention as the points."""
         if _np_dtype(kx) != self.dtype:
             raise TypeError("cufinufft plan.dtype and kx dtypes do not match.")
         if ky is not None and _np_dtype(ky) != self.dtype:
@@ -184,7 +188,24 @@ class cufinufft:
         if kz is not None:
             fpts_axes.insert(0, _ptr(kz))
             self.references.append(kz)
-        ier = self._set_pts(M, *fpts_axes[:3], 0, None, None, None, self.plan)
+        N, tgt = 0, [None, None, None]
+        if self._finufft_type == 3:
+            if s is None:
+                raise TypeError("type 3 needs target frequencies s (t, u)")
+            freqs = [f for f in (s, t, u) if f is not None]
+            if len(freqs) != self.dim:
+                raise TypeError("type 3 needs one frequency array per dimension")
+            for f in freqs:
+                if _np_dtype(f) != self.dtype:
+                    raise TypeError("cufinufft plan.dtype and frequency dtypes do not match.")
+            N = _size(freqs[0])
+            if any(_size(f) != N for f in freqs):
+                raise TypeError("Number of elements in s, t, u must be equal")
+            # library axis order: the last C-ordered axis is x
+            real_p = ctypes.POINTER(ctypes.c_double if self.dtype == np.float64 else ctypes.c_float)
+            tgt = [ctypes.cast(c_void_p(_ptr(f)), real_p) for f in freqs[::-1]] + [None] * (3 - self.dim)
+            self.references.extend(freqs)
+        ier = self._set_pts(M, *fpts_axes[:3], N, *tgt, self.plan)
         if ier != 0:
             raise RuntimeError('Error setting non-uniform points.')
 

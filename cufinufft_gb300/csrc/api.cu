@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <initializer_list>
 #include <type_traits>
 #include <new>
 #include <vector>
@@ -43,9 +44,11 @@ int default_opts(int type, int dim, cufinufft_opts* opts) {
   opts->gpu_kerevalmeth = 0;
   opts->gpu_device_id = 0;
   if (dim < 1 || dim > 3) return CUFINUFFT_ERR_ARG;
-  if (type == 1) opts->gpu_method = 2;
+  // type 3 spreads as type 1 does (the reference reserves type 3 and
+  // returns 1 here)
+  if (type == 1 || type == 3) opts->gpu_method = 2;
   else if (type == 2) opts->gpu_method = 1;
-  else return CUFINUFFT_ERR_GENERIC;  // type 3 is not implemented (reference returns 1)
+  else return CUFINUFFT_ERR_GENERIC;
   return 0;
 }
 
@@ -102,6 +105,27 @@ template <typename T> static void release(Plan<T>* p) {
     delete p->lo;
     p->lo = nullptr;
   }
+  Plan<T>** const t3[2] = {&p->t3_spread, &p->t3_inner};
+  for (Plan<T>** q : t3) {
+    if (*q) {
+      release(*q);
+      delete *q;
+      *q = nullptr;
+    }
+  }
+  for (int k = 0; k < 3; ++k) {
+    cudaFree(p->t3_xp[k]);
+    cudaFree(p->t3_tau[k]);
+    p->t3_xp[k] = p->t3_tau[k] = nullptr;
+  }
+  cudaFree(p->t3_pre);
+  cudaFree(p->t3_post);
+  cudaFree(p->t3_c);
+  cudaFree(p->t3_grid);
+  cudaFree(p->t3_part);
+  p->t3_pre = p->t3_post = p->t3_c = p->t3_grid = nullptr;
+  p->t3_part = nullptr;
+  p->t3_capM = p->t3_capN = p->t3_capG = 0;
   cudaFree(p->n_idx);
   p->n_idx = nullptr;
   for (int k = 0; k < 3; ++k) {
@@ -885,7 +909,16 @@ static int bank_order(Plan<T>* p, int method, const int bs[3], int nbins, BankOr
   CFG_CUDA(cudaMemsetAsync(p->cls_count, 0, sizeof(int) * n, p->stream));
   o->cls_count = p->cls_count;
   o->ncls = ncls;
-  o->tx = bs[0] + p->sp.ns - 1;
+  // the tile row length the interpolation kernel will index with: FP32 tiles
+  // moved by bulk copies widen odd rows by one cell (bulk_tile_x), so the
+  // classes must be taken modulo that pitch, or consecutive points of a bin
+  // stop falling in distinct banks
+  int tx = bs[0] + p->sp.ns - 1;
+  if (is_single<T>() && p->type == 2 && (bs[0] & 1) == 0 && (tx & 1)) {
+    const char* v = std::getenv("CUFINUFFT_TMA");
+    if (!(v && v[0] == '0') && tma_encoder() != nullptr) tx += 1;
+  }
+  o->tx = tx;
   o->ty = p->dim > 1 ? bs[1] + p->sp.ns - 1 : 1;
   return 0;
 }
@@ -895,6 +928,8 @@ static int build_subproblems(Plan<T>* p);
 
 static int setpts_chain(Plan<double>* p, int M, const double* x, const double* y, const double* z);
 static int execute_chain(Plan<double>* p, double2* c, double2* fk);
+template <typename T>
+static int execute_t3(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk);
 
 template <typename T>
 static int setpts_impl(Plan<T>* p, int M, const T* x, const T* y, const T* z) {
@@ -1144,6 +1179,7 @@ static int execute_impl(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
   if constexpr (std::is_same<T, double>::value) {
     if (p->lo) return execute_chain(p, c, fk);
   }
+  if (p->type == 3) return execute_t3(p, c, fk);
   if (const int e = take_status(p)) return e;
   if (p->timing || !p->planned || !graphs_enabled()) return execute_direct(p, c, fk);
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1385,6 +1421,223 @@ static int execute_chain(Plan<double>* p, double2* c, double2* fk) {
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Type 3 (nonuniform points to nonuniform frequencies; type3.cu has the
+// method).  makeplan keeps the parameters; setpts measures the extents of
+// the points and frequencies, sizes the rescaled grid (nf >= 2 sigma S X /
+// pi + ns + 1 per axis, with x' = (x - C)/gam in [-pi, pi) and gam = nf /
+// (2 sigma S)), and makes a spread-only plan onto that grid and an inner
+// type-2 plan over it (both with this plan's kernel); execute runs
+// prephase -> spread -> type 2 -> phase / phihat.
+template <typename T>
+static int makeplan_t3(Plan<T>* p, int dim, int iflag, int ntransf, double tol, int maxbatchsize,
+                       const cufinufft_opts* opts) {
+  p->type = 3;
+  p->dim = dim;
+  p->width_rule = width_rule_now();
+  if (opts) p->opts = *opts;
+  else default_opts(3, dim, &p->opts);
+  if (p->opts.gpu_spreadinterponly) return CUFINUFFT_ERR_ARG;
+  int ier = setup_spreader(tol, p->opts.upsampfac, p->opts.gpu_kerevalmeth, is_single<T>(), &p->sp,
+                           p->width_rule, dim);
+  if (ier > 1) return ier;
+  p->iflag = iflag >= 0 ? 1 : -1;
+  p->ntransf = ntransf;
+  if (maxbatchsize == 0) maxbatchsize = std::min(ntransf, 8);
+  p->maxbatch = std::min(maxbatchsize, ntransf);
+  p->t3_tol = tol;
+  p->method = 2;
+  CFG_CUDA(cudaStreamCreate(&p->own));
+  p->stream = p->own;
+  CFG_CUDA(cudaMalloc(&p->t3_part, sizeof(double) * 2 * (size_t)minmax_partials()));
+  p->planned = true;
+  return 0;
+}
+
+// Minimum and maximum of a[0..n) (device), on the plan stream.
+template <typename T>
+static int extent(Plan<T>* p, const T* a, long long n, double* lo, double* hi) {
+  *lo = *hi = 0.0;
+  if (n <= 0) return 0;
+  int nb = 0;
+  CFG_CUDA(launch_minmax<T>(a, n, p->t3_part, &nb, p->stream));
+  std::vector<double> h(2 * (size_t)nb);
+  CFG_CUDA(cudaMemcpyAsync(h.data(), p->t3_part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, p->stream));
+  CFG_CUDA(cudaStreamSynchronize(p->stream));
+  double a0 = h[0], a1 = h[1];
+  for (int b = 1; b < nb; ++b) {
+    a0 = std::min(a0, h[2 * b]);
+    a1 = std::max(a1, h[2 * b + 1]);
+  }
+  if (!std::isfinite(a0) || !std::isfinite(a1)) return CUFINUFFT_ERR_ARG;
+  *lo = a0;
+  *hi = a1;
+  return 0;
+}
+
+template <typename T>
+static int grow(T** buf, size_t* cap, size_t n) {
+  if (n <= *cap && *buf) return 0;
+  cudaFree(*buf);
+  *buf = nullptr;
+  *cap = 0;
+  CFG_CUDA(cudaMalloc(buf, sizeof(T) * std::max<size_t>(n, 1)));
+  *cap = n;
+  return 0;
+}
+
+template <typename T>
+static int setpts_t3(Plan<T>* p, int M, const T* x, const T* y, const T* z, int Nt, const T* s, const T* t,
+                     const T* u) {
+  if (!p->planned) return CUFINUFFT_ERR_GENERIC;
+  if (M < 0 || Nt < 0) return CUFINUFFT_ERR_ARG;
+  const T* xs[3] = {x, y, z};
+  const T* ss[3] = {s, t, u};
+  for (int k = 0; k < p->dim; ++k)
+    if ((M > 0 && !xs[k]) || (Nt > 0 && !ss[k])) return CUFINUFFT_ERR_ARG;
+  p->pts_set = false;
+  ++p->version;
+  const double sigma = p->opts.upsampfac;
+  const int nss = p->sp.ns + 1;
+  int nf[3] = {1, 1, 1};
+  long long cells = 1;
+  for (int k = 0; k < p->dim; ++k) {
+    double xl, xh, sl, sh;
+    int e = extent(p, xs[k], M, &xl, &xh);
+    if (e) return e;
+    e = extent(p, ss[k], Nt, &sl, &sh);
+    if (e) return e;
+    double X = 0.5 * (xh - xl), S = 0.5 * (sh - sl);
+    p->t3_C[k] = 0.5 * (xh + xl);
+    p->t3_D[k] = 0.5 * (sh + sl);
+    if (X == 0.0) X = S == 0.0 ? 1.0 : 1.0 / S;
+    if (S == 0.0) S = 1.0 / X;
+    const double nfd = 2.0 * sigma * S * X / M_PI + nss;
+    if (!(nfd < (double)(1 << 22))) return CUFINUFFT_ERR_ARG;  // the grid would not fit
+    int n = std::max((int)nfd, 2 * nss);
+    n = next235beven(n, 1);
+    nf[k] = n;
+    cells *= n;
+    p->t3_h[k] = 2.0 * M_PI / n;
+    p->t3_gam[k] = n / (2.0 * sigma * S);
+  }
+  if (cells > (1LL << 28)) return CUFINUFFT_ERR_ARG;
+  p->M = M;
+  p->t3_N = Nt;
+  // spread-only plan onto the rescaled grid and the inner type-2 plan, made
+  // again when the grid changes
+  auto same = [&](const Plan<T>* q) {
+    return q && q->nf[0] == nf[0] && q->nf[1] == nf[1] && q->nf[2] == nf[2];
+  };
+  if (!same(p->t3_spread) || !p->t3_inner || p->t3_inner->N[0] != nf[0] || p->t3_inner->N[1] != nf[1] ||
+      p->t3_inner->N[2] != nf[2]) {
+    Plan<T>** const t3[2] = {&p->t3_spread, &p->t3_inner};
+  for (Plan<T>** q : t3) {
+      if (*q) {
+        release(*q);
+        delete *q;
+        *q = nullptr;
+      }
+    }
+    p->t3_spread = new (std::nothrow) Plan<T>();
+    p->t3_inner = new (std::nothrow) Plan<T>();
+    if (!p->t3_spread || !p->t3_inner) return CUFINUFFT_ERR_ALLOC;
+    p->t3_spread->device = p->t3_inner->device = p->device;
+    cufinufft_opts o1 = p->opts;
+    o1.gpu_spreadinterponly = 1;
+    int e = makeplan_impl<T>(p->t3_spread, 1, p->dim, nf, p->iflag, p->ntransf, p->t3_tol, p->maxbatch, &o1,
+                             &p->sp);
+    if (e) return e;
+    cufinufft_opts o2;
+    default_opts(2, p->dim, &o2);
+    o2.upsampfac = p->opts.upsampfac;
+    o2.gpu_kerevalmeth = p->opts.gpu_kerevalmeth;
+    o2.gpu_device_id = p->opts.gpu_device_id;
+    o2.gpu_method = 0;  // the library's choice for the inner interpolation
+    e = makeplan_impl<T>(p->t3_inner, 2, p->dim, nf, p->iflag, p->ntransf, p->t3_tol, p->maxbatch, &o2,
+                         &p->sp);
+    if (e) return e;
+    plan_use_stream(p->t3_spread, p->stream);
+    plan_use_stream(p->t3_inner, p->stream);
+  }
+  for (int k = 0; k < 3; ++k) p->nf[k] = nf[k];
+  if ((size_t)M > p->t3_capM || !p->t3_pre) {
+    for (int k = 0; k < 3; ++k) {
+      cudaFree(p->t3_xp[k]);
+      p->t3_xp[k] = nullptr;
+    }
+    cudaFree(p->t3_pre);
+    cudaFree(p->t3_c);
+    p->t3_pre = p->t3_c = nullptr;
+    p->t3_capM = 0;
+    const size_t n = (size_t)std::max(M, 1);
+    for (int k = 0; k < p->dim; ++k) CFG_CUDA(cudaMalloc(&p->t3_xp[k], sizeof(T) * n));
+    CFG_CUDA(cudaMalloc(&p->t3_pre, sizeof(cplx_t<T>) * n));
+    CFG_CUDA(cudaMalloc(&p->t3_c, sizeof(cplx_t<T>) * n * (size_t)p->ntransf));
+    p->t3_capM = n;
+  }
+  if ((size_t)Nt > p->t3_capN || !p->t3_post) {
+    for (int k = 0; k < 3; ++k) {
+      cudaFree(p->t3_tau[k]);
+      p->t3_tau[k] = nullptr;
+    }
+    cudaFree(p->t3_post);
+    p->t3_post = nullptr;
+    p->t3_capN = 0;
+    const size_t n = (size_t)std::max(Nt, 1);
+    for (int k = 0; k < p->dim; ++k) CFG_CUDA(cudaMalloc(&p->t3_tau[k], sizeof(T) * n));
+    CFG_CUDA(cudaMalloc(&p->t3_post, sizeof(cplx_t<T>) * n));
+    p->t3_capN = n;
+  }
+  {
+    const int e = grow(&p->t3_grid, &p->t3_capG, (size_t)cells * p->ntransf);
+    if (e) return e;
+  }
+  Type3Phase<T> ph;
+  std::memset(&ph, 0, sizeof(ph));
+  ph.dim = p->dim;
+  ph.sgn = p->iflag;
+  for (int k = 0; k < p->dim; ++k) {
+    ph.C[k] = p->t3_C[k];
+    ph.D[k] = p->t3_D[k];
+    ph.hg[k] = p->t3_h[k] * p->t3_gam[k];
+    CFG_CUDA(launch_affine<T>(xs[k], M, p->t3_C[k], 1.0 / p->t3_gam[k], p->t3_xp[k], p->stream));
+    CFG_CUDA(launch_affine<T>(ss[k], Nt, p->t3_D[k], ph.hg[k], p->t3_tau[k], p->stream));
+  }
+  for (int k = 0; k < p->dim; ++k) ph.x[k] = xs[k];
+  CFG_CUDA(launch_prephase<T>(ph, M, p->t3_pre, p->stream));
+  for (int k = 0; k < p->dim; ++k) ph.x[k] = ss[k];
+  FseriesNodes nodes;
+  fseries_nodes(p->sp, &nodes);
+  CFG_CUDA(launch_postfactor<T>(ph, nodes, Nt, p->t3_post, p->stream));
+  int e = setpts_impl(p->t3_spread, M, p->t3_xp[0], p->t3_xp[1], p->t3_xp[2]);
+  if (e) return e;
+  e = setpts_impl(p->t3_inner, Nt, p->t3_tau[0], p->t3_tau[1], p->t3_tau[2]);
+  if (e) return e;
+  // the caller's arrays may be released once setpts returns
+  CFG_CUDA(cudaStreamSynchronize(p->stream));
+  p->pts_set = true;
+  return 0;
+}
+
+template <typename T>
+static int execute_t3(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
+  if (!p->planned || !p->pts_set) return CUFINUFFT_ERR_GENERIC;
+  if ((p->M > 0 && !c) || (p->t3_N > 0 && !fk)) return CUFINUFFT_ERR_ARG;
+  if (p->t3_N == 0) return 0;
+  if (p->M == 0) {
+    CFG_CUDA(cudaMemsetAsync(fk, 0, sizeof(cplx_t<T>) * (size_t)p->t3_N * p->ntransf, p->stream));
+    return 0;
+  }
+  CFG_CUDA(launch_cmul_rows<T>(c, p->t3_pre, p->M, p->ntransf, p->t3_c, p->stream));
+  int e = execute_impl(p->t3_spread, p->t3_c, p->t3_grid);
+  if (e) return e;
+  e = execute_impl(p->t3_inner, fk, p->t3_grid);
+  if (e) return e;
+  CFG_CUDA(launch_cmul_rows<T>(fk, p->t3_post, p->t3_N, p->ntransf, fk, p->stream));
+  return 0;
+}
+
 // Entry points for the batch (batch.cu): a plan's whole execute, and moving
 // a plan's work, cuFFT plans included, to another stream.
 template <typename T>
@@ -1401,6 +1654,12 @@ int plan_use_stream(Plan<T>* p, cudaStream_t s) {
     p->stream = s;
     return e;
   }
+  Plan<T>* const t3[2] = {p->t3_spread, p->t3_inner};
+  for (Plan<T>* q : t3)
+    if (q) {
+      const int e = plan_use_stream(q, s);
+      if (e) return e;
+    }
   p->stream = s;
   if (p->have_fft) CFG_CUFFT(cufftSetStream(p->fft, s));
   if (p->have_fft_rem) CFG_CUFFT(cufftSetStream(p->fft_rem, s));
@@ -1521,6 +1780,7 @@ static int build_subproblems(Plan<T>* p) {
 template <typename T>
 static int set_layout_impl(Plan<T>* p, int method, const int bsz[3], int maxsub) {
   if (!p->planned) return CUFINUFFT_ERR_GENERIC;
+  if (p->type == 3) return CUFINUFFT_ERR_METHOD;  // type 3 lays out its inner plans itself
   ++p->version;  // the sorted arrays and bin tables are about to move
   // method 5: method 2 spreading over cell-ordered points (cell-run kernel)
   const bool cell = method == 5;
@@ -1701,6 +1961,7 @@ static std::vector<cufinufft_tune_entry> tune_candidates(const Plan<T>* p) {
 
 template <typename T>
 static int autotune_impl(Plan<T>* p, cufinufft_tune_entry* out, int max_out, int* n_out) {
+  if (p->type == 3) return CUFINUFFT_ERR_METHOD;
   if (!p->planned || !p->pts_set) return CUFINUFFT_ERR_GENERIC;
   std::vector<cufinufft_tune_entry> cand = tune_candidates(p);
   if (n_out) *n_out = 0;
@@ -1761,6 +2022,7 @@ static int autotune_impl(Plan<T>* p, cufinufft_tune_entry* out, int max_out, int
 
 template <typename T>
 static int features_impl(Plan<T>* p, float* f) {
+  if (p->type == 3) return CUFINUFFT_ERR_METHOD;
   if (!p->planned || !p->pts_set) return CUFINUFFT_ERR_GENERIC;
   int fb[3] = {1, 1, 1}, nb[3] = {1, 1, 1};
   long long nbins = 1;
@@ -1876,14 +2138,20 @@ static int makeplan_entry(int type, int dim, int* nmodes, int iflag, int ntransf
   *plan = h;
   Plan<T>* p = &h->p;
   p->device = opts ? opts->gpu_device_id : 0;
-  if (type != 1 && type != 2) {
+  if (type != 1 && type != 2 && type != 3) {
     p->type = type;
     p->dim = dim;
-    return CUFINUFFT_ERR_GENERIC;  // type 3 is not implemented (src/cufinufft.cu:533)
+    return CUFINUFFT_ERR_GENERIC;
   }
   DeviceGuard g(p->device);
   if (!g.ok) return CUFINUFFT_ERR_CUDA;
   int ier;
+  if (type == 3) {
+    // implemented here; the reference returns 1 (src/cufinufft.cu:533-536)
+    ier = makeplan_t3<T>(p, dim, iflag, ntransf, tol, maxbatchsize, opts);
+    if (ier) release(p);
+    return ier;
+  }
   if constexpr (std::is_same<T, double>::value) {
     if (chain_wanted(type, tol, opts)) {
       ier = makeplan_chain(p, type, dim, nmodes, iflag, ntransf, tol, maxbatchsize, opts);
@@ -1903,10 +2171,12 @@ using cfg::DeviceGuard;
 
 template <typename H>
 static int setpts_entry(H* h, int M, decltype(h->p.d[0]) x, decltype(h->p.d[0]) y,
-                        decltype(h->p.d[0]) z) {
+                        decltype(h->p.d[0]) z, int N, decltype(h->p.d[0]) s, decltype(h->p.d[0]) t,
+                        decltype(h->p.d[0]) u) {
   if (h == nullptr) return CUFINUFFT_ERR_GENERIC;
   DeviceGuard g(h->p.device);
   if (!g.ok) return CUFINUFFT_ERR_CUDA;
+  if (h->p.type == 3) return cfg::setpts_t3(&h->p, M, x, y, z, N, s, t, u);
   return cfg::setpts_impl(&h->p, M, x, y, z);
 }
 
@@ -2033,13 +2303,11 @@ int cufinufftf_makeplan(int type, int dim, int* nmodes, int iflag, int ntransf, 
 
 int cufinufft_setpts(int M, double* x, double* y, double* z, int N, double* s, double* t, double* u,
                      cufinufft_plan plan) {
-  (void)N; (void)s; (void)t; (void)u;
-  return setpts_entry(plan, M, x, y, z);
+  return setpts_entry(plan, M, x, y, z, N, s, t, u);
 }
 int cufinufftf_setpts(int M, float* x, float* y, float* z, int N, float* s, float* t, float* u,
                       cufinufftf_plan plan) {
-  (void)N; (void)s; (void)t; (void)u;
-  return setpts_entry(plan, M, x, y, z);
+  return setpts_entry(plan, M, x, y, z, N, s, t, u);
 }
 
 int cufinufft_execute(cuDoubleComplex* c, cuDoubleComplex* fk, cufinufft_plan plan) {

@@ -226,6 +226,7 @@ static int batch_make(Batch<T>* b, int nplans, Plan<T>** plans) {
       return CUFINUFFT_ERR_ARG;  // one type, dimension, kernel width and device per batch
     if (p->opts.gpu_kerevalmeth != 0) return CUFINUFFT_ERR_ARG;
     if (p->spread_only) return CUFINUFFT_ERR_ARG;  // the batch runs whole transforms
+    if (p->type == 3) return CUFINUFFT_ERR_ARG;    // types 1 and 2 only
     b->plans.push_back(p);
   }
   CFG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));

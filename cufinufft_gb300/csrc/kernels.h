@@ -143,6 +143,31 @@ struct FseriesNodes {
   double f[kMaxNQuad / 2];   // (ns/2) w_n phi(z_n)
   int q;
 };
+
+// type3.cu -- elementwise steps of the type-3 transform.  x: the points the
+// step reads (sources for the prephase, target frequencies for the post
+// factor); C, D: centres of the sources and targets; hg = h gam, the scale
+// from target frequency to the inner type-2 frequency; sgn = +-1.
+template <typename T>
+struct Type3Phase {
+  const T* x[3];
+  double C[3], D[3], hg[3];
+  double sgn;
+  int dim;
+};
+int minmax_partials();
+template <typename T>
+cudaError_t launch_minmax(const T* a, long long n, double* partial, int* nblocks, cudaStream_t s);
+template <typename T>
+cudaError_t launch_affine(const T* a, long long n, double centre, double scale, T* out, cudaStream_t s);
+template <typename T>
+cudaError_t launch_prephase(const Type3Phase<T>& a, long long n, cplx_t<T>* pre, cudaStream_t s);
+template <typename T>
+cudaError_t launch_postfactor(const Type3Phase<T>& a, const FseriesNodes& nodes, long long n, cplx_t<T>* post,
+                              cudaStream_t s);
+template <typename T>
+cudaError_t launch_cmul_rows(const cplx_t<T>* u, const cplx_t<T>* w, long long n, int ntr, cplx_t<T>* v,
+                             cudaStream_t s);
 // fac[d][i] = 1 / fhat_d(|i - N_d/2|), i = 0..N_d-1, FP64 evaluation.
 template <typename T>
 cudaError_t launch_fseries(const FseriesNodes& nodes, int dim, const int nf[3], const int N[3],

@@ -86,6 +86,21 @@ template <typename T> struct Plan {
   cplx_t<float>* c32 = nullptr;
   size_t c32_cap = 0;
   cplx_t<float>* fk32 = nullptr;
+  // type 3: a spread-only plan onto the rescaled grid and an inner type-2
+  // plan over that grid, the extents of sources and targets, phases
+  Plan<T>* t3_spread = nullptr;
+  Plan<T>* t3_inner = nullptr;
+  double t3_tol = 0;
+  double t3_C[3] = {0, 0, 0}, t3_D[3] = {0, 0, 0}, t3_gam[3] = {1, 1, 1}, t3_h[3] = {1, 1, 1};
+  int t3_N = 0;                       // targets
+  T* t3_xp[3] = {nullptr, nullptr, nullptr};   // rescaled sources (scratch of setpts)
+  T* t3_tau[3] = {nullptr, nullptr, nullptr};  // inner type-2 frequencies (scratch of setpts)
+  cplx_t<T>* t3_pre = nullptr;        // [M] prephase
+  cplx_t<T>* t3_post = nullptr;       // [N] phase over phihat
+  cplx_t<T>* t3_c = nullptr;          // [ntransf M] prephased strengths
+  cplx_t<T>* t3_grid = nullptr;       // [ntransf nf] spread grid
+  size_t t3_capM = 0, t3_capN = 0, t3_capG = 0;
+  double* t3_part = nullptr;          // min/max partials (device)
   int* h_total = nullptr;  // pinned readback of the subproblem count
   // interpolation tile-wait status (SpreadArgs::status): host-mapped, two ints
   int* h_status = nullptr;

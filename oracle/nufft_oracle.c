@@ -467,3 +467,31 @@ void orc_dirft_type2(int dim, int ms, int mt, int mu, const double* x,
     out[2 * m + 1] = ai;
   }
 }
+
+/* FP64 direct sum of the type-3 transform (nonuniform to nonuniform), the
+ * accuracy reference for type 3: f[m] = sum_j c[j] exp(i*sgn*(s_k.x_j)) at
+ * the targets k = targets[m].  The reference library reserves type 3 in its
+ * interface (src/cufinufft.cu:533-536) without implementing it, so this sum
+ * is the only check.  x/y/z: M source points; s/t/u: target frequencies. */
+void orc_dirft_type3(int dim, int M, const double* x, const double* y,
+                     const double* z, const double* c, const double* s,
+                     const double* t, const double* u, int iflag,
+                     int ntargets, const long long* targets, double* out) {
+  double sgn = iflag >= 0 ? 1.0 : -1.0;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int m = 0; m < ntargets; ++m) {
+    long long k = targets[m];
+    double ar = 0.0, ai = 0.0;
+    for (int j = 0; j < M; ++j) {
+      double ph = s[k] * x[j];
+      if (dim > 1) ph += t[k] * y[j];
+      if (dim > 2) ph += u[k] * z[j];
+      ph *= sgn;
+      double cs = cos(ph), sn = sin(ph);
+      ar += c[2 * j] * cs - c[2 * j + 1] * sn;
+      ai += c[2 * j] * sn + c[2 * j + 1] * cs;
+    }
+    out[2 * m] = ar;
+    out[2 * m + 1] = ai;
+  }
+}

@@ -71,6 +71,8 @@ def lib() -> ctypes.CDLL:
                                                                              _ll_p, _d_p]
             L.orc_dirft_type2.argtypes = [ctypes.c_int] * 4 + [_d_p] * 4 + [ctypes.c_int, ctypes.c_int,
                                                                              _ll_p, _d_p]
+            L.orc_dirft_type3.argtypes = [ctypes.c_int, ctypes.c_int] + [_d_p] * 7 + [
+                ctypes.c_int, ctypes.c_int, _ll_p, _d_p]
             L.orc_num_threads.restype = ctypes.c_int
             L.orc_set_num_threads.argtypes = [ctypes.c_int]
             _LIB = L
@@ -298,3 +300,26 @@ def rel_l2(est, ref) -> float:
     est = np.asarray(est).ravel()
     ref = np.asarray(ref).ravel()
     return float(np.linalg.norm(est - ref) / np.linalg.norm(ref))
+
+
+def direct_type3(x, y, z, c, s, t, u, iflag: int, target_idx) -> np.ndarray:
+    """FP64 direct sum of the type-3 transform f_k = sum_j c_j exp(i sgn s_k.x_j)
+    at targets ``target_idx`` (sources x, y, z; target frequencies s, t, u;
+    unused axes None)."""
+    px = _f64(x)
+    M = px.size
+    dim = 1 + (y is not None) + (z is not None)
+    ps = _f64(s)
+    dummy = np.zeros(max(M, 1))
+    dummy_t = np.zeros(max(ps.size, 1))
+    py = _f64(y) if y is not None else dummy
+    pz = _f64(z) if z is not None else dummy
+    pt = _f64(t) if t is not None else dummy_t
+    pu = _f64(u) if u is not None else dummy_t
+    cc = _c128(c).reshape(M)
+    idx = np.ascontiguousarray(np.asarray(target_idx, dtype=np.int64))
+    out = np.zeros(idx.size, dtype=np.complex128)
+    lib().orc_dirft_type3(dim, M, _dp(px), _dp(py), _dp(pz), _dp(cc.view(np.float64)), _dp(ps),
+                          _dp(pt), _dp(pu), int(iflag), idx.size, idx.ctypes.data_as(_ll_p),
+                          _dp(out.view(np.float64)))
+    return out

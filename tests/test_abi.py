@@ -66,9 +66,14 @@ def test_default_opts_match_reference(lib, dim, ntype):
         assert o.gpu_nstreams == 0 and o.gpu_device_id == 0
 
 
-def test_default_opts_type3_not_implemented(lib):
+def test_default_opts_type3(lib):
+    # the reference reserves type 3 and returns 1 here (src/cufinufft.cu:
+    # 685-689); type 3 is implemented in this library and spreads as type 1
     from cufinufft_gb300._cufinufft import NufftOpts, _default_opts
-    assert _default_opts(3, 2, NufftOpts()) == 1
+    o = NufftOpts()
+    assert _default_opts(3, 2, o) == 0
+    assert o.gpu_method == 2 and o.upsampfac == 2.0
+    assert _default_opts(4, 2, NufftOpts()) == 1
 
 
 def test_makeplan_argument_checks_need_no_device(lib):

@@ -195,9 +195,13 @@ def test_c_abi_error_returns():
     from cufinufft_gb300 import _cufinufft as L
     mk, sp, ex, de = _raw(True)
     nmodes = (ctypes.c_int * 3)(16, 16, 16)
-    # type 3 is reserved: makeplan returns 1 (src/cufinufft.cu:533-536)
+    # type 3 is implemented here (the reference's makeplan returns 1 for it,
+    # src/cufinufft.cu:533-536); an unknown type still returns 1
     plan = ctypes.c_void_p(None)
-    assert mk(3, 3, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), None) == 1
+    assert mk(3, 3, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), None) == 0
+    assert de(plan) == 0
+    plan = ctypes.c_void_p(None)
+    assert mk(4, 3, nmodes, 1, 1, 1e-6, 0, ctypes.byref(plan), None) == 1
     assert de(plan) == 0
     # a method the dimension does not offer: execute returns 2
     # (src/3d/spread3d_wrapper.cu:155-157)
