@@ -237,13 +237,13 @@ static bool use_line_fft(const Plan<T>* p) {
   return true;
 }
 
-// Pruned power-of-two passes (halffft.cu): every axis nf = 2M with M a power
-// of two in [64, 1024] and at most M modes (always so at upsampfac 2).  The
-// default where they apply; CUFINUFFT_FFT=cufft (or line) selects another.
+// Pruned power-of-two passes (halffft.cu): every axis nf a power of two in
+// [256, 2048] with at most nf/2 modes (always so at upsampfac 2); selected
+// by CUFINUFFT_FFT=half.
 template <typename T>
 static bool use_half_fft(const Plan<T>* p) {
   const char* v = std::getenv("CUFINUFFT_FFT");
-  if (v && std::strcmp(v, "half") != 0) return false;
+  if (!v || std::strcmp(v, "half") != 0) return false;
   for (int k = 0; k < p->dim; ++k)
     if (!half_fft_size_ok(p->nf[k]) || 2 * p->N[k] > p->nf[k]) return false;
   return true;
@@ -281,7 +281,10 @@ static std::vector<HalfPass<T>> half_passes(const Plan<T>* p, cplx_t<T>* fk, int
     HalfPass<T> a;
     std::memset(&a, 0, sizeof(a));
     a.kind = kind;
-    a.M = p->nf[axis] / 2;
+    a.Mp = half_fft_mp(p->nf[axis]);
+    a.F = p->nf[axis] / a.Mp;
+    a.Fb = std::min(a.F, 4);
+    a.dir = p->iflag;
     a.N = p->N[axis];
     a.tw = p->tw[axis];
     a.ntr = B;
@@ -289,7 +292,6 @@ static std::vector<HalfPass<T>> half_passes(const Plan<T>* p, cplx_t<T>* fk, int
     a.Na = 1;
     return a;
   };
-  auto cols_pitch = [](int n) { return ((n + 15) / 16) * 16 + 4; };  // 4 mod 16: conflict-free gathers
   std::vector<HalfPass<T>> v;
   if (p->type == 2) {
     cplx_t<T>* t1 = p->fw;
@@ -319,7 +321,7 @@ static std::vector<HalfPass<T>> half_passes(const Plan<T>* p, cplx_t<T>* fk, int
       y.out_tr = p->dim == 2 ? Nf : (long long)N2 * L1 * L0;
       y.out_row = L0;
       y.out_plane = L1 * L0;
-      y.pitch = cols_pitch(N1);
+      y.pitch = half_col_pitch<T>(N1, y.Mp);
       v.push_back(y);
     }
     if (p->dim == 3) {
@@ -331,7 +333,7 @@ static std::vector<HalfPass<T>> half_passes(const Plan<T>* p, cplx_t<T>* fk, int
       z.out = p->fw2;
       z.out_tr = Nf;
       z.out_row = L1 * L0;
-      z.pitch = cols_pitch(N2);
+      z.pitch = half_col_pitch<T>(N2, z.Mp);
       v.push_back(z);
     }
     return v;
@@ -347,7 +349,7 @@ static std::vector<HalfPass<T>> half_passes(const Plan<T>* p, cplx_t<T>* fk, int
     z.out = s2;
     z.out_tr = (long long)N2 * L1 * L0;
     z.out_row = L1 * L0;
-    z.pitch = cols_pitch((int)(L2 / 2));
+    z.pitch = half_col_pitch<T>(z.Mp, z.Mp);
     v.push_back(z);
   }
   if (p->dim >= 2) {
@@ -362,7 +364,7 @@ static std::vector<HalfPass<T>> half_passes(const Plan<T>* p, cplx_t<T>* fk, int
     y.out_tr = (long long)N2 * N1 * L0;
     y.out_row = L0;
     y.out_plane = (long long)N1 * L0;
-    y.pitch = cols_pitch((int)(L1 / 2));
+    y.pitch = half_col_pitch<T>(y.Mp, y.Mp);
     v.push_back(y);
   }
   HalfPass<T> x = base(kHalfT1Rows, 0);

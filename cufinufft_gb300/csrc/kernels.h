@@ -217,17 +217,20 @@ struct LineArgs {
   int fac_on_out;
 };
 
-// Pruned power-of-two passes (halffft.cu) for grids nf = 2M, M = 32 Q with
-// Q in {2, 4, 8, 16, 32}: per axis two M-point FFTs (one per output or input
-// parity) over the lines that hold modes.
+// Pruned power-of-two passes (halffft.cu) for grids nf in {256, ..., 2048}
+// with at most nf/2 modes per axis: per axis F = nf / Mp warp FFTs of Mp
+// points (one per output or input class q, grid position F r + q) over the
+// lines that hold modes.
 enum HalfKind { kHalfT2Rows = 0, kHalfT2Cols = 1, kHalfT1Cols = 2, kHalfT1Rows = 3 };
 template <typename T>
 struct HalfPass {
   int kind;
-  int M, N;                   // FFT size (the axis has 2M grid points) and modes on this axis
+  int Mp, F, Fb;              // per-warp FFT size, classes (the axis has F Mp grid points),
+                              // classes per block of the strided type-2 pass
+  int N;                      // modes on this axis
   const cplx_t<T>* in;
   cplx_t<T>* out;
-  const cplx_t<T>* tw;        // W^t = exp(dir 2 pi i t / 2M), t < 2M
+  const cplx_t<T>* tw;        // W^t = exp(dir 2 pi i t / nf), t < nf
   int ntr;                    // transforms; transform t at in + t in_tr, out + t out_tr
   long long in_tr, out_tr;
   // rows passes: nlines contiguous lines, line g at in + g in_row / out + g out_row;
@@ -242,10 +245,15 @@ struct HalfPass {
   // outer index o at in + o in_plane / out + o out_plane
   int ncols, nouter;
   long long in_plane, out_plane;
-  int pitch;                  // shared-memory pitch of a column (elements)
+  int pitch;                  // shared-memory pitch of a column (elements), half_col_pitch
+  int dir;                    // sign of the exponent (+1 or -1)
 };
 template <typename T> cudaError_t launch_half_pass(const HalfPass<T>& a, cudaStream_t s);
 bool half_fft_size_ok(int nf);
+int half_fft_mp(int nf);
+// Pitch of the column buffers of the strided passes for n values per column
+// and Mp-point transforms (at least both, bank-conflict offset added).
+template <typename T> int half_col_pitch(int n, int Mp);
 
 template <typename T> int line_fft_cap();
 template <typename T> int line_fft_p2_elems();

@@ -1,5 +1,5 @@
-"""Pruned power-of-two FFT passes (csrc/halffft.cu, the default where every
-fine-grid side is a power of two in [128, 2048]) against cuFFT over the
+"""Pruned power-of-two FFT passes (csrc/halffft.cu, CUFINUFFT_FFT=half, for
+fine grids whose sides are powers of two in [256, 2048]) against cuFFT over the
 whole grid (CUFINUFFT_FFT=cufft) and against the oracle.  Both compute the
 same transform; the passes split each 2M-point line into two M-point FFTs
 over the mode lines only, so results agree to the plan precision's FFT
@@ -14,10 +14,10 @@ from tests import nufft_cases as NC
 pytestmark = pytest.mark.gpu
 
 CASES = [
-    # modes (N1 fastest), type
-    ((509,), 1), ((509,), 2), ((1024,), 2),
-    ((63, 64), 1), ((63, 64), 2), ((128, 127), 1), ((128, 127), 2), ((512, 256), 2),
-    ((64, 63, 62), 1), ((64, 63, 62), 2), ((128, 128, 64), 1),
+    # modes (N1 fastest), type; fine grids 256 .. 2048 per side
+    ((509,), 1), ((509,), 2), ((1024,), 2), ((127,), 1),
+    ((127, 128), 1), ((127, 128), 2), ((256, 255), 1), ((256, 255), 2), ((1024, 512), 1),
+    ((1024, 512), 2), ((128, 127, 126), 1), ((128, 127, 126), 2),
 ]
 
 
@@ -34,7 +34,7 @@ def test_half_fft_matches_cufft(monkeypatch, modes, ntype, single):
     ntr = 3
     data = (NC.strengths(rng, M, ntr) if ntype == 1 else NC.coeffs(rng, modes, ntr)).astype(cdt)
     iflag = -1 if ntype == 1 else 1   # the opposite signs of the defaults
-    monkeypatch.delenv("CUFINUFFT_FFT", raising=False)
+    monkeypatch.setenv("CUFINUFFT_FFT", "half")
     a, ia = NC.run_gpu(ntype, modes, pts, data, tol, single, ntr=ntr, iflag=iflag, maxbatchsize=2)
     monkeypatch.setenv("CUFINUFFT_FFT", "cufft")
     b, ib = NC.run_gpu(ntype, modes, pts, data, tol, single, ntr=ntr, iflag=iflag, maxbatchsize=2)
@@ -47,7 +47,8 @@ def test_half_fft_matches_cufft(monkeypatch, modes, ntype, single):
     assert same < (2e-5 if single else 1e-10), same
 
 
-def test_half_fft_not_taken_for_other_sizes():
+def test_half_fft_not_taken_for_other_sizes(monkeypatch):
+    monkeypatch.setenv("CUFINUFFT_FFT", "half")
     rng = np.random.default_rng(2)
     pts = NC.points(rng, 2, 500, dtype=np.float32)
     c = NC.strengths(rng, 500).astype(np.complex64)
