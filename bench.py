@@ -987,6 +987,9 @@ def main():
                          "'reference' is the reference's ns = ceil(-log10(tol/10))")
     ap.add_argument("--no-extras", action="store_true",
                     help="default workload only: skip the 3D cluster and uneven-batch lines")
+    ap.add_argument("--points", type=int, default=None,
+                    help="number of points of the uniform / clustered workloads (smaller cases "
+                         "for profiling; the default is the workload's own)")
     args = ap.parse_args()
     if args.impl == "ours":
         args.warmup = max(args.warmup, 3)
@@ -1000,6 +1003,12 @@ def main():
                     int(os.environ.get("LOCAL_RANK", 0)))
         return
     w = WORKLOADS[args.workload]()
+    if args.points is not None:
+        if not hasattr(w, "M"):
+            raise SystemExit("--points applies to the uniform and clustered workloads")
+        # a smaller case of the same workload (profiling captures)
+        w.M = int(args.points)
+        w.desc = w.desc + f" (reduced to M={w.M})"
     world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":

@@ -29,6 +29,7 @@
 
 #include "device_common.cuh"
 #include "kernels.h"
+#include "tc_common.cuh"
 
 namespace cfg {
 
@@ -981,6 +982,212 @@ size_t run_bytes(int ns, const BinTables& bt) {
          nw * 32 * sizeof(cplx_t<T>);
 }
 
+// ---------------------------------------------------------------------------
+// Tensor-core cell-run spreading (3D FP32, ns <= 8; CUFINUFFT_TC_SPREAD=1).
+// A chunk of n <= 32 points on one cell adds, to the cell's ns^3 taps,
+//   S[ix][iy][iz] = sum_q (c_q kx_q[ix]) (ky_q[iy] kz_q[iz]),
+// a product D = A B^T with A[m][q] = ky_q[iy] kz_q[iz] (m = iy + ns iz,
+// M = 128 rows, ns^2 used) and B[n][q] = kx_q[ix] Re/Im(c_q) (n = 2 ix + re/im,
+// N = 16): tcgen05.mma kind::tf32 with K = 8 points per instruction, each
+// operand split into a TF32 part and its FP32 remainder (hi hi + hi lo + lo
+// hi, FP32 accumulation in tensor memory), the accumulator read back by the
+// first warpgroup and added to the tile planes.  The CTA walks the
+// subproblem's dense prefix chunk by chunk (a chunk opens a cell whose
+// first 32-point window runs at least dense_run(3) points, or continues the
+// previous chunk's cell); the points after it are spread point by point as
+// in k_spread_sm_wc.
+constexpr int kTcK = 32;                   // points per chunk (4 MMA K-steps)
+constexpr int kTcWaitPolls = 1 << 22;      // bounded waits on the MMA barrier
+
+__host__ __device__ constexpr size_t tc_operand_floats() {
+  return 2 * (kTcK / 8) * 1024 + 2 * (kTcK / 8) * 128;  // A hi/lo, B hi/lo
+}
+template <int NS>
+__host__ __device__ constexpr size_t tc_stage_floats() {
+  return (size_t)kTcK * 3 * NS + 2 * kTcK;  // kernel rows, strengths
+}
+inline size_t tc_run_bytes(int ns, const BinTables& bt) {
+  return (tc_operand_floats() + (size_t)kTcK * 3 * ns + 2 * kTcK + 2 * tile_cells(3, ns, bt.bs)) * sizeof(float);
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kSpreadThreads)
+k_spread_sm_run_tc(SpreadArgs<float> a) {
+  constexpr int HD = horner_degree<float>(NS);
+  constexpr int KV = 3 * NS;
+  if (a.sub_dense && !a.sub_dense[blockIdx.x]) return;  // sparse: done by k_spread_sm_wc
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ unsigned tmem_base;
+  __shared__ int s_n, s_key;
+  const SubTile st = sub_tile_block<3, NS>(a.bins, blockIdx.x);
+  float* A_hi = reinterpret_cast<float*>(smem_raw);
+  float* A_lo = A_hi + (kTcK / 8) * 1024;
+  float* B_hi = A_lo + (kTcK / 8) * 1024;
+  float* B_lo = B_hi + (kTcK / 8) * 128;
+  float* kv = B_lo + (kTcK / 8) * 128;                 // [kTcK][3 NS]
+  float2* cv = reinterpret_cast<float2*>(kv + kTcK * KV);  // [kTcK]
+  float* re = reinterpret_cast<float*>(cv + kTcK);
+  float* im = re + st.ntile;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int t = blockIdx.y;
+  const float2* cin = a.c_in + (size_t)t * a.M;
+  for (int i = tid; i < 2 * st.ntile; i += blockDim.x) re[i] = 0.f;
+  if (tid == 0) mbar_init(&bar, 1);
+  if (warp == 0) tmem_alloc(&tmem_base, 32);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const unsigned taddr = tmem_base;
+  constexpr unsigned idesc = umma_idesc_tf32(128, 16);
+  constexpr int kMinRun = dense_run(3);
+  int cs = 0, prev_key = -1;
+  unsigned phase = 0;
+  bool healthy = true;
+  while (healthy) {  // block-uniform
+    if (warp == 0) {
+      const int q = cs + lane;
+      const bool valid = q < st.np;
+      int key = -1;
+      if (valid) {
+        const int p = st.p0 + q;
+        key = (a.pts.i0[0][p] - st.ox) + st.TX * ((a.pts.i0[1][p] - st.oy) + st.TY * (a.pts.i0[2][p] - st.oz));
+      }
+      const int key0 = __shfl_sync(0xffffffffu, key, 0);
+      const unsigned same = __ballot_sync(0xffffffffu, valid && key == key0);
+      const int nrun = same == 0xffffffffu ? 32 : __ffs(~same) - 1;
+      const bool dense = cs < st.np && (nrun >= kMinRun || key0 == prev_key);
+      if (lane == 0) {
+        s_n = dense ? nrun : 0;
+        s_key = key0;
+      }
+    }
+    __syncthreads();
+    const int n = s_n, key0 = s_key;
+    if (n == 0) break;
+    // the chunk's kernel rows and strengths
+    if (tid < n) {
+      const int p = st.p0 + cs + tid;
+      float kr[NS];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        kernel_row<float, NS, HD>(a.pts.d[d][p], a.kc, kr);
+#pragma unroll
+        for (int j = 0; j < NS; ++j) kv[tid * KV + d * NS + j] = kr[j];
+      }
+      cv[tid] = cin[a.pts.idx[p]];
+    }
+    __syncthreads();
+    // operands, K padded to kTcK with zero points
+    for (int e = tid; e < 128 * kTcK; e += blockDim.x) {
+      const int m = e & 127, q = e >> 7;
+      float v = 0.f;
+      if (m < NS * NS && q < n) v = kv[q * KV + NS + m % NS] * kv[q * KV + 2 * NS + m / NS];
+      float hi, lo;
+      tf32_split(v, hi, lo);
+      const int off = (q >> 3) * 1024 + umma_kmaj_off(m, q & 7);
+      A_hi[off] = hi;
+      A_lo[off] = lo;
+    }
+    for (int e = tid; e < 16 * kTcK; e += blockDim.x) {
+      const int nn = e & 15, q = e >> 4;
+      const int ix = nn >> 1;
+      float v = 0.f;
+      if (ix < NS && q < n) v = kv[q * KV + ix] * ((nn & 1) ? cv[q].y : cv[q].x);
+      float hi, lo;
+      tf32_split(v, hi, lo);
+      const int off = (q >> 3) * 128 + umma_kmaj_off(nn, q & 7);
+      B_hi[off] = hi;
+      B_lo[off] = lo;
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const int ksteps = (n + 7) >> 3;
+      for (int s = 0; s < ksteps; ++s) {
+        const uint64_t ah = umma_sdesc(A_hi + s * 1024, kUmmaLbo, kUmmaSbo);
+        const uint64_t al = umma_sdesc(A_lo + s * 1024, kUmmaLbo, kUmmaSbo);
+        const uint64_t bh = umma_sdesc(B_hi + s * 128, kUmmaLbo, kUmmaSbo);
+        const uint64_t bl = umma_sdesc(B_lo + s * 128, kUmmaLbo, kUmmaSbo);
+        umma_tf32(taddr, ah, bh, idesc, s > 0 ? 1u : 0u);
+        umma_tf32(taddr, ah, bl, idesc, 1u);
+        umma_tf32(taddr, al, bh, idesc, 1u);
+      }
+      umma_commit(&bar);
+    }
+    bool done = mbar_wait(&bar, phase, kTcWaitPolls);
+    if (!done) {
+      // record the stall; wait again (bounded) so no MMA is in flight when
+      // the tile or tensor memory is reused or freed
+      status_set(a.status, 0);
+      done = mbar_wait(&bar, phase, kTcWaitPolls);
+      if (!done) status_set(a.status, 1);
+    }
+    phase ^= 1u;
+    healthy = __syncthreads_and(done ? 1 : 0) != 0;
+    tc_fence_after();
+    if (healthy && warp < 4) {
+      float d[16];
+      tmem_ld16(taddr + ((unsigned)(32 * warp) << 16), d);
+      const int m = 32 * warp + lane;
+      if (m < NS * NS) {
+        const int base = key0 + st.TX * ((m % NS) + st.TY * (m / NS));
+#pragma unroll
+        for (int ix = 0; ix < NS; ++ix) {
+          re[base + ix] += d[2 * ix];
+          im[base + ix] += d[2 * ix + 1];
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+    prev_key = key0;
+    cs += n;
+  }
+  // the points after the dense prefix, one at a time (lanes over x taps)
+  {
+    constexpr int L = spread_lanes<NS>();
+    constexpr int PPW = 32 / L;
+    const int g = lane / L, j = lane % L;
+    const bool tap = j < NS;
+    const int jj = tap ? j : 0;
+    const int nwb = blockDim.x >> 5;
+    for (int base = cs + warp * PPW; base < st.np; base += nwb * PPW) {
+      const int pl = base + g;
+      const bool valid = g < PPW && pl < st.np;
+      const int p = st.p0 + (valid ? pl : st.np - 1);
+      const int lx = a.pts.i0[0][p] - st.ox, ly = a.pts.i0[1][p] - st.oy, lz = a.pts.i0[2][p] - st.oz;
+      const float kx = kernel_tap<float, NS, HD>(a.pts.d[0][p], jj, a.kc);
+      const float ky = kernel_tap<float, NS, HD>(a.pts.d[1][p], jj, a.kc);
+      const float kz = kernel_tap<float, NS, HD>(a.pts.d[2][p], jj, a.kc);
+      const float2 v = cin[a.pts.idx[p]];
+      const float vr = v.x * kx, vi = v.y * kx;
+      const int off0 = (lz * st.TY + ly) * st.TX + lx + jj;
+#pragma unroll 1
+      for (int dz = 0; dz < NS; ++dz) {
+        const float kzv = __shfl_sync(0xffffffffu, kz, g * L + dz);
+#pragma unroll
+        for (int dy = 0; dy < NS; ++dy) {
+          const float w = __shfl_sync(0xffffffffu, ky, g * L + dy) * kzv;
+          if (tap && valid) {
+            const int off = off0 + (dz * st.TY + dy) * st.TX;
+            atomicAdd(re + off, vr * w);
+            atomicAdd(im + off, vi * w);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  plane_flush<float>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(taddr, 32);
+}
+
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
 k_interp_sm_wc(SpreadArgs<T> a) {
@@ -1064,6 +1271,13 @@ cudaError_t prepare_smem(K kernel, size_t bytes) {
   return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+// CUFINUFFT_TC_SPREAD=1: the dense runs of 3D FP32 cell-run subproblems go
+// to the tensor-core kernel (k_spread_sm_run_tc).
+inline bool tc_spread_enabled() {
+  const char* v = std::getenv("CUFINUFFT_TC_SPREAD");
+  return v && v[0] == '1';
+}
+
 // Kernel family per stage (SpreadArgs::variant 0 = the measured default):
 // spreading is warp-cooperative for both methods; interpolation is
 // warp-cooperative for method 1 and one-thread-per-point for method 2.
@@ -1090,6 +1304,15 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
         cudaError_t e = prepare_smem(k_spread_sm_wc<T, DIM, NS>, smw);
         if (e != cudaSuccess) return e;
         k_spread_sm_wc<T, DIM, NS><<<dim3(a.bins.nsub, a.ntr), kSpreadThreads, smw, s>>>(a);
+        if constexpr (sizeof(T) == 4 && DIM == 3 && NS <= 8) {
+          if (tc_spread_enabled()) {
+            const size_t smt = tc_run_bytes(NS, a.bins);
+            e = prepare_smem(k_spread_sm_run_tc<NS>, smt);
+            if (e != cudaSuccess) return e;
+            k_spread_sm_run_tc<NS><<<dim3(a.bins.nsub, a.ntr), kSpreadThreads, smt, s>>>(a);
+            return cudaGetLastError();
+          }
+        }
         const size_t sm = run_bytes<T, DIM>(NS, a.bins);
         e = prepare_smem(k_spread_sm_run<T, DIM, NS>, sm);
         if (e != cudaSuccess) return e;

@@ -130,3 +130,30 @@ def test_cell_run_rejected_for_type2():
     plan.set_pts(x, x)
     with pytest.raises(RuntimeError):
         plan.set_layout(5, (16, 16), 1024)
+
+
+@pytest.mark.parametrize("tol", [1e-3, 1e-5, 1e-6])
+@pytest.mark.parametrize("bins", [(8, 8, 8), (16, 16, 2)])
+def test_tensor_core_cell_run_matches(monkeypatch, tol, bins):
+    """CUFINUFFT_TC_SPREAD=1: the dense runs of 3D FP32 cell-run subproblems
+    are summed by tcgen05 MMAs (TF32 split in two, FP32 accumulation) instead
+    of CUDA-core FMAs.  The sums are the same to FP32 rounding, so the result
+    matches the CUDA-core cell-run kernel and the oracle (2e-5, the FP32
+    bound), with multiple transforms and widths 4 to 7 (<= 8 is the kernel's
+    limit)."""
+    rng = np.random.default_rng(int(-np.log10(tol)) + bins[2])
+    modes = (24, 20, 16)
+    M, ntr = 20000, 2
+    pts = _clustered(rng, 3, M, np.float32, [2 * m for m in modes])
+    c = NC.strengths(rng, M, ntr).astype(np.complex64)
+    monkeypatch.delenv("CUFINUFFT_TC_SPREAD", raising=False)
+    ref_cc, _ = _run(modes, pts, c, tol, True, ntr, layout=(5, bins, 1024), gpu_method=2)
+    monkeypatch.setenv("CUFINUFFT_TC_SPREAD", "1")
+    out, info = _run(modes, pts, c, tol, True, ntr, layout=(5, bins, 1024), gpu_method=2)
+    assert info["cell_order"] == 1
+    err = np.linalg.norm(out.ravel() - ref_cc.ravel()) / np.linalg.norm(ref_cc.ravel())
+    assert err < 2e-5, err
+    ref = NC.oracle_nufft(1, modes, [p.astype(np.float64) for p in pts], c.astype(np.complex128),
+                          tol, True, ntr=ntr)
+    err_o = np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
+    assert err_o < 2e-5, err_o
