@@ -486,7 +486,11 @@ def run_ours(args, w: Workload, rank, world, local_rank, extra=False):
     inp, out, args_ce = _io_tensors(w, data_dev, M, dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     plan, tune, selector_info = _tuned_plan(w, dev, stream, opts, pts_dev, args_ce, flush,
-                                            args.method == 0)
+                                            args.method == 0 and args.layout is None)
+    if args.layout is not None:
+        # a fixed layout for the timed plan (profiling a given kernel)
+        lm, lx, ly, lz, lc = (int(v) for v in args.layout.split(","))
+        plan.set_layout(lm, (lx, ly, lz)[:w.dim], lc)
     with torch.cuda.stream(stream):
         plan.execute(*args_ce)
     torch.cuda.synchronize()
@@ -987,6 +991,9 @@ def main():
                          "'reference' is the reference's ns = ceil(-log10(tol/10))")
     ap.add_argument("--no-extras", action="store_true",
                     help="default workload only: skip the 3D cluster and uneven-batch lines")
+    ap.add_argument("--layout", default=None,
+                    help="method,bx,by,bz,maxsub: a fixed layout for the timed plan instead of the "
+                         "tuned one (set_layout; method 5 = cell-run spread)")
     ap.add_argument("--points", type=int, default=None,
                     help="number of points of the uniform / clustered workloads (smaller cases "
                          "for profiling; the default is the workload's own)")

@@ -1033,6 +1033,13 @@ k_spread_sm_run_tc(SpreadArgs<float> a) {
   const int t = blockIdx.y;
   const float2* cin = a.c_in + (size_t)t * a.M;
   for (int i = tid; i < 2 * st.ntile; i += blockDim.x) re[i] = 0.f;
+  // rows NS^2 .. 127 of A stay zero for every chunk: written once
+  for (int e = tid; e < (128 - NS * NS) * kTcK; e += blockDim.x) {
+    const int m = NS * NS + e % (128 - NS * NS), q = e / (128 - NS * NS);
+    const int off = (q >> 3) * 1024 + umma_kmaj_off(m, q & 7);
+    A_hi[off] = 0.f;
+    A_lo[off] = 0.f;
+  }
   if (tid == 0) mbar_init(&bar, 1);
   if (warp == 0) tmem_alloc(&tmem_base, 32);
   tc_fence_before();
@@ -1065,24 +1072,19 @@ k_spread_sm_run_tc(SpreadArgs<float> a) {
     __syncthreads();
     const int n = s_n, key0 = s_key;
     if (n == 0) break;
-    // the chunk's kernel rows and strengths
-    if (tid < n) {
-      const int p = st.p0 + cs + tid;
-      float kr[NS];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        kernel_row<float, NS, HD>(a.pts.d[d][p], a.kc, kr);
-#pragma unroll
-        for (int j = 0; j < NS; ++j) kv[tid * KV + d * NS + j] = kr[j];
-      }
-      cv[tid] = cin[a.pts.idx[p]];
+    // the chunk's kernel values (one tap per thread) and strengths
+    for (int e = tid; e < n * KV; e += blockDim.x) {
+      const int q = e / KV, r = e - q * KV;
+      const int p = st.p0 + cs + q;
+      kv[e] = kernel_tap<float, NS, HD>(a.pts.d[r / NS][p], r % NS, a.kc);
     }
+    if (tid < n) cv[tid] = cin[a.pts.idx[st.p0 + cs + tid]];
     __syncthreads();
-    // operands, K padded to kTcK with zero points
-    for (int e = tid; e < 128 * kTcK; e += blockDim.x) {
-      const int m = e & 127, q = e >> 7;
+    // operands, K padded to kTcK with zero points (rows >= NS^2 are zero)
+    for (int e = tid; e < NS * NS * kTcK; e += blockDim.x) {
+      const int m = e % (NS * NS), q = e / (NS * NS);
       float v = 0.f;
-      if (m < NS * NS && q < n) v = kv[q * KV + NS + m % NS] * kv[q * KV + 2 * NS + m / NS];
+      if (q < n) v = kv[q * KV + NS + m % NS] * kv[q * KV + 2 * NS + m / NS];
       float hi, lo;
       tf32_split(v, hi, lo);
       const int off = (q >> 3) * 1024 + umma_kmaj_off(m, q & 7);
