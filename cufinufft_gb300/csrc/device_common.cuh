@@ -179,6 +179,50 @@ __device__ __forceinline__ T kernel_tap(T d, int j, const KernelCoeffs<T>& kc) {
   return es_eval(kc.c * x * x, kc);
 }
 
+// ---- double-float arithmetic (FP64 plans without FP64 units) -------------
+// A value is an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2):
+// ~48 bits of mantissa.  Error-free transformations: two_sum (Knuth) and
+// the FMA product error; every step rounds explicitly, so the compiler never
+// contracts or reassociates them.
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF df_from(double v) {
+  DF r;
+  r.h = __double2float_rn(v);
+  r.l = __double2float_rn(v - (double)r.h);
+  return r;
+}
+__device__ __forceinline__ double df_to(DF a) { return (double)a.h + (double)a.l; }
+// s + e = a + b exactly
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ DF df_renorm(float s, float e) {
+  DF r;
+  r.h = __fadd_rn(s, e);
+  r.l = __fsub_rn(e, __fsub_rn(r.h, s));
+  return r;
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  float s, e;
+  two_sum(a.h, b.h, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.l, b.l));
+  return df_renorm(s, e);
+}
+// a * b to ~2^-47 relative (the lo*lo term is dropped)
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return df_renorm(p, e);
+}
+// acc + a * b
+__device__ __forceinline__ DF df_fma(DF a, DF b, DF acc) { return df_add(acc, df_mul(a, b)); }
+
 // ---- packed FP32 pairs (sm_100+) -----------------------------------------
 // c + a * b on both halves of a float2 in one instruction (CUDA's
 // __ffma2_rn); each half is the IEEE fma of that half, so results equal two

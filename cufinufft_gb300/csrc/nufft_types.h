@@ -38,12 +38,21 @@ constexpr int kMaxHornerRows = kMaxNS + 4;  // degree <= ns + 3
 // z^(deg-k) for tap j.  The coefficients travel inside the kernel's
 // parameter block, so the unrolled evaluation reads them straight from the
 // constant bank.
+// FP64 plans also carry the fitted polynomials as FP32 pairs (hi + lo, the
+// double-float interpolation kernel evaluates them without FP64 units).
+template <typename T> struct DFCoef {};
+template <> struct DFCoef<double> {
+  float hi[kMaxHornerRows * kMaxNS];
+  float lo[kMaxHornerRows * kMaxNS];
+};
+
 template <typename T> struct KernelCoeffs {
   T beta, c;
   T e_beta, bl2e;                    // e^beta and beta log2(e) (FP32 kernel evaluation)
   int horner;
   const T* coef_g;                   // device copy, read by kernel_tap (runtime tap index)
   T coef[kMaxHornerRows * kMaxNS];
+  DFCoef<T> df;
 };
 
 // Bin-sorted points in plan memory (written by setpts).

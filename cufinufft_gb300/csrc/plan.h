@@ -217,8 +217,13 @@ inline SpreadArgs<T> spread_args(Plan<T>* p) {
   a.kc.bl2e = (T)(p->sp.beta * 1.44269504088896340736);
   a.kc.horner = p->horner.empty() ? 0 : 1;
   a.kc.coef_g = p->horner_d;
-  for (size_t k = 0; k < p->horner.size() && k < (size_t)(kMaxHornerRows * kMaxNS); ++k)
+  for (size_t k = 0; k < p->horner.size() && k < (size_t)(kMaxHornerRows * kMaxNS); ++k) {
     a.kc.coef[k] = p->horner[k];
+    if constexpr (sizeof(T) == 8) {
+      a.kc.df.hi[k] = (float)p->horner[k];
+      a.kc.df.lo[k] = (float)(p->horner[k] - (double)a.kc.df.hi[k]);
+    }
+  }
   a.g.Nf = grid_cells(p);
   a.M = p->M;
   a.variant = p->variant;

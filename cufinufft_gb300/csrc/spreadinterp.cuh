@@ -582,6 +582,140 @@ k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) 
 }
 
 // ---------------------------------------------------------------------------
+// Double-float interpolation for FP64 plans (CUFINUFFT_FP64_DF=1).  GB300's
+// FP64 units are a small fraction of its FP32 throughput, and the FP64 tap
+// loop (2 FMAs per tap, ns^d taps) plus the FP64 kernel evaluation (a Horner
+// step per tap value and degree) bound FP64 interpolation.  Here the tile
+// (loaded as for k_interp_sm) is converted in place to FP32 pairs (hi, lo per
+// component, the same 16 bytes per cell), the kernel rows are evaluated in
+// double-float (the fitted polynomials from FP32-pair coefficients, or the
+// FP64 exp form rounded to pairs), and the taps accumulate as a float sum
+// plus a float error term (two-sum and FMA product errors): ~2^-46
+// relative, ample for tol >= 1e-13, with FP32 instructions only.
+struct DFAcc {
+  float s, t;
+  __device__ __forceinline__ void zero() { s = t = 0.f; }
+  // += a * b
+  __device__ __forceinline__ void add_prod(DF a, float bh, float bl) {
+    const float p = __fmul_rn(a.h, bh);
+    float pe = __fmaf_rn(a.h, bh, -p);
+    pe = __fmaf_rn(a.h, bl, pe);
+    pe = __fmaf_rn(a.l, bh, pe);
+    float ns, e;
+    two_sum(s, p, ns, e);
+    s = ns;
+    t = __fadd_rn(t, __fadd_rn(e, pe));
+  }
+  __device__ __forceinline__ DF value() const { return df_renorm(s, t); }
+};
+
+// Kernel value phi(d - ns/2 + j) in double-float.
+template <int NS, int HD>
+__device__ __forceinline__ DF df_kernel_tap(double d, int j, const KernelCoeffs<double>& kc) {
+  if (kc.horner) {
+    const DF z = df_from(2.0 * d - 1.0);
+    DF v;
+    v.h = kc.df.hi[j];
+    v.l = kc.df.lo[j];
+#pragma unroll
+    for (int k = 1; k <= HD; ++k) {
+      DF c;
+      c.h = kc.df.hi[k * NS + j];
+      c.l = kc.df.lo[k * NS + j];
+      v = df_fma(v, z, c);
+    }
+    return v;
+  }
+  const double x = d - 0.5 * NS + j;
+  return df_from(es_value(kc.c * x * x, kc.beta));
+}
+
+template <int DIM, int NS>
+__global__ void __launch_bounds__(kInterpThreads, kInterpBlocksF64)
+k_interp_sm_df(SpreadArgs<double> a, const __grid_constant__ CUtensorMap gmap, int tma) {
+  using C = double2;
+  constexpr int HD = horner_degree<double>(NS);
+  constexpr int NY = DIM > 1 ? NS : 1;
+  constexpr int NZ = DIM > 2 ? NS : 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) unsigned long long tile_bar;
+  C* tile = reinterpret_cast<C*>(tma ? smem_align128(smem_raw) : smem_raw);
+  if (tma && threadIdx.x == 0) mbar_init(&tile_bar, 1);
+  SubTile st = sub_tile_hdr<DIM, NS>(a.bins, blockIdx.x);
+  if (tma) __syncthreads();
+  const int t = blockIdx.y;
+  const C* src = a.fw_in + (size_t)t * a.g.Nf;
+  const bool bulk = tma && tile_in_grid(st, a.g);
+  if (bulk && threadIdx.x == 0) tile_copy_start<double, DIM>(tile, &gmap, st, t, &tile_bar);
+  if (!bulk) tile_load_periodic<double>(tile, src, st, a.g);
+  if (bulk) tile_copy_wait<double>(tile, &tile_bar, src, st, a.g, a.status, a.tma_wait_test);
+  __syncthreads();
+  // the tile in place as FP32 pairs: (re hi, re lo, im hi, im lo) per cell
+  float4* tdf = reinterpret_cast<float4*>(tile);
+  for (int i = threadIdx.x; i < st.ntile; i += blockDim.x) {
+    const C v = tile[i];
+    const DF r = df_from(v.x), m = df_from(v.y);
+    tdf[i] = make_float4(r.h, r.l, m.h, m.l);
+  }
+  __syncthreads();
+  const int p_end = st.p0 + st.np;
+  for (int p = st.p0 + threadIdx.x; p < p_end; p += blockDim.x) {
+    const int lx = a.pts.i0[0][p] - st.ox;
+    const int ly = DIM > 1 ? a.pts.i0[1][p] - st.oy : 0;
+    const int lz = DIM > 2 ? a.pts.i0[2][p] - st.oz : 0;
+    DF kx[NS], ky[NY];
+    const double d1 = a.pts.d[0][p];
+#pragma unroll
+    for (int j = 0; j < NS; ++j) kx[j] = df_kernel_tap<NS, HD>(d1, j, a.kc);
+    if (DIM > 1) {
+      const double d2 = a.pts.d[1][p];
+#pragma unroll
+      for (int j = 0; j < NY; ++j) ky[j] = df_kernel_tap<NS, HD>(d2, j, a.kc);
+    } else {
+      ky[0].h = 1.f;
+      ky[0].l = 0.f;
+    }
+    const double d3 = DIM > 2 ? a.pts.d[2][p] : 0.0;
+    DFAcc are, aim;
+    are.zero();
+    aim.zero();
+#pragma unroll 1
+    for (int dz = 0; dz < NZ; ++dz) {
+      DF kz;
+      if (DIM > 2) kz = df_kernel_tap<NS, HD>(d3, dz, a.kc);
+      const float4* plane = tdf + ((lz + dz) * st.TY + ly) * st.TX + lx;
+#pragma unroll
+      for (int dy = 0; dy < NY; ++dy) {
+        const float4* row = plane + dy * st.TX;
+        DFAcc rre, rim;
+        rre.zero();
+        rim.zero();
+#pragma unroll
+        for (int dx = 0; dx < NS; ++dx) {
+          const float4 g = row[dx];
+          rre.add_prod(kx[dx], g.x, g.y);
+          rim.add_prod(kx[dx], g.z, g.w);
+        }
+        DF w = ky[dy];
+        if (DIM > 2) w = df_mul(w, kz);
+        const DF vr = rre.value(), vi = rim.value();
+        are.add_prod(w, vr.h, vr.l);
+        aim.add_prod(w, vi.h, vi.l);
+      }
+    }
+    C o;
+    o.x = df_to(are.value());
+    o.y = df_to(aim.value());
+    a.c_out[(size_t)t * a.M + a.pts.idx[p]] = o;
+  }
+}
+
+inline bool fp64_df_enabled() {
+  const char* v = std::getenv("CUFINUFFT_FP64_DF");
+  return v && v[0] == '1';
+}
+
+// ---------------------------------------------------------------------------
 // Warp-cooperative variants.  A warp works on PPW = 32 / L points at a time;
 // the L >= ns lanes of a point cover its x taps, so every warp-wide memory
 // instruction touches PPW contiguous runs of ns cells (one row of each
@@ -1365,6 +1499,14 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
         if (e != cudaSuccess) return e;
         if (smb <= (size_t)optin) sm = smb;
         else tma = 0;
+      }
+    }
+    if constexpr (sizeof(T) == 8) {
+      if (!wc && fp64_df_enabled()) {
+        cudaError_t e = prepare_smem(k_interp_sm_df<DIM, NS>, sm);
+        if (e != cudaSuccess) return e;
+        k_interp_sm_df<DIM, NS><<<dim3(a.bins.nsub, a.ntr), kInterpThreads, sm, s>>>(a, gmap, tma);
+        return cudaGetLastError();
       }
     }
     cudaError_t e = wc ? prepare_smem(k_interp_sm_wc<T, DIM, NS>, sm)
