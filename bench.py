@@ -34,6 +34,7 @@ from __future__ import annotations
 
 import argparse
 import collections
+import ctypes
 import json
 import math
 import os
@@ -65,6 +66,7 @@ class Workload:
         self.single, self.tol, self.desc = single, tol, desc
         self.ntransf = ntransf
         self.acc_n = acc_n
+        self.upsampfac = 2.0   # of the timed plan (--upsampfac); the oracle's same-width check follows it
         self._pts = None
 
     @property
@@ -249,10 +251,36 @@ def committed_traffic(key: str):
 
 
 # --------------------------------------------------------------------------
+def atomic_roofline(taps: int, k_ms: float, single: bool) -> dict:
+    """The spread's own ceiling: algorithmic tap updates (M ns^d per
+    transform, a complex add each, i.e. two real adds) per second against the
+    device's measured shared-memory atomicAdd rate (the library's
+    cufinufft_atomic_rate probe, one lane per address).  Dense cells summed in
+    registers (cell-run layout) issue fewer atomics than the algorithmic count,
+    so `frac` can pass 1 there."""
+    from cufinufft_gb300 import _cufinufft as cl
+    rates = {}
+    for kind, key in ((0, "shared_f32"), (1, "shared_i32"), (2, "global_red_v2_f32"),
+                      (3, "shared_u64")):
+        r = ctypes.c_double(0.0)
+        if cl.atomic_rate(kind, ctypes.byref(r)) != 0:
+            raise RuntimeError("cufinufft_atomic_rate failed")
+        rates[key] = r.value
+    achieved = 2.0 * taps / (k_ms / 1e3)
+    peak = rates["shared_f32"] if single else None
+    return {"bound": "shared-atomic", "unit": "real adds/s", "achieved": achieved,
+            "algorithmic_adds": 2 * taps, "peak": peak,
+            "frac": achieved / peak if peak else None,
+            "measured_rates": rates,
+            "note": "peak = shared FP32 atomicAdd lane-ops/s measured on this device by "
+                    "cufinufft_atomic_rate; FP64 plans: no FP32 peak applies"}
+
+
 def oracle_plan(w: Workload, cores: int, ns=None):
     from oracle import oracle as O
     O.set_num_threads(cores)
-    plan = O.OraclePlan(w.ntype, w.modes, 1 if w.ntype == 1 else -1, w.tol, w.single, ns=ns)
+    plan = O.OraclePlan(w.ntype, w.modes, 1 if w.ntype == 1 else -1, w.tol, w.single, ns=ns,
+                        upsampfac=w.upsampfac if ns is not None else 2.0)
     plan.fft_workers = cores
     return plan
 
@@ -456,6 +484,8 @@ def _tuned_plan(w: Workload, dev, stream, opts, pts_dev, args_ce, flush, tuned: 
 def _tuned_opts(args, w: Workload):
     # tuned form: the library chooses the method (gpu_method 0) unless given
     opts = {"gpu_method": args.method}
+    if args.upsampfac is not None:
+        opts["upsampfac"] = args.upsampfac
     if args.kerevalmeth is not None:
         opts["gpu_kerevalmeth"] = args.kerevalmeth
     elif args.method == 0 and not w.single:
@@ -655,9 +685,11 @@ def run_ours(args, w: Workload, rank, world, local_rank, extra=False):
     e2e_ms = e2e_serial(args.steps)
     e2e_pipe_ms = e2e_pipelined(args.steps)
     barrier()
-    scale = float(np.abs(out_first).max())
+    # the same transform: equal up to the order of FP32/FP64 atomic additions,
+    # which the deconvolution amplifies at low upsampling factors
     for k in range(2):
-        if not np.allclose(out_host[k].numpy(), out_first, rtol=0, atol=1e-4 * scale):
+        dif = np.linalg.norm((out_host[k].numpy() - out_first).ravel())
+        if dif > (10 * w.tol + 1e-5) * np.linalg.norm(out_first.ravel()):
             raise RuntimeError("e2e output differs from the device-resident run")
 
     dev_ms, e2e_ms, e2e_pipe_ms = reduce_max([dev_ms, e2e_ms, e2e_pipe_ms], dist, dev)
@@ -696,6 +728,8 @@ def run_ours(args, w: Workload, rank, world, local_rank, extra=False):
                                 f"per execute there)",
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)",
             "stage_ms": {k: v / nb for k, v in stages.items() if k != "batches"}}
+    if w.ntype == 1:
+        roof["atomic"] = atomic_roofline(M * info["ns"] ** w.dim * w.ntransf, k_ms, w.single)
 
     cpu = None
     if world == 1 and not args.no_cpu:
@@ -983,6 +1017,9 @@ def main():
     ap.add_argument("--method", type=int, default=0,
                     help="gpu_method for the timed plan (0 = chosen by the library)")
     ap.add_argument("--kerevalmeth", type=int, default=None)
+    ap.add_argument("--upsampfac", type=float, default=None,
+                    help="upsampling factor of the timed plan (the reference's opts.upsampfac: "
+                         "2.0 by default, 1.25 the low-upsampling grid)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the direct-sum check")
     ap.add_argument("--no-plain", action="store_true", help="skip the default-options plan")
@@ -1010,6 +1047,8 @@ def main():
                     int(os.environ.get("LOCAL_RANK", 0)))
         return
     w = WORKLOADS[args.workload]()
+    if args.upsampfac is not None:
+        w.upsampfac = args.upsampfac
     if args.points is not None:
         if not hasattr(w, "M"):
             raise SystemExit("--points applies to the uniform and clustered workloads")

@@ -73,7 +73,7 @@ class PlanInfo(ctypes.Structure):
         "nsubprob", "kerevalmeth")] + [("beta", c_double), ("es_c", c_double),
                                        ("line_fft", c_int), ("cell_order", c_int),
                                        ("width_rule", c_int), ("chain_fp32", c_int),
-                                       ("half_fft", c_int)]
+                                       ("half_fft", c_int), ("fp64_df", c_int)]
 
 
 CufinufftPlan = c_void_p
@@ -216,3 +216,8 @@ mlp_grad.restype = c_int
 mlp_adam = lib.cufinufft_mlp_adam
 mlp_adam.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_float, c_void_p]
 mlp_adam.restype = c_int
+
+# Measured accumulation ceilings (shared FP32 / int32 atomicAdd, global 8-byte reduction).
+atomic_rate = lib.cufinufft_atomic_rate
+atomic_rate.argtypes = [c_int, c_double_p]
+atomic_rate.restype = c_int

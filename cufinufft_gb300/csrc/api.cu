@@ -738,6 +738,12 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
     p->h_status[0] = p->h_status[1] = 0;
     CFG_CUDA(cudaHostGetDevicePointer(&p->d_status, p->h_status, 0));
     if (const char* v = std::getenv("CUFINUFFT_TMA_WAIT_TEST")) p->tma_wait_test = v[0] == '1';
+    if constexpr (sizeof(T) == 8) {
+      // double-float interpolation: ~2^-46 relative, below every tol >= 1e-13;
+      // CUFINUFFT_FP64_DF=0 keeps FP64 instructions, =1 takes it at any tol
+      const char* v = std::getenv("CUFINUFFT_FP64_DF");
+      p->fp64_df = v && v[0] == '0' ? 0 : (v && v[0] == '1' ? 1 : (tol >= 1e-13 ? 1 : 0));
+    }
   }
 
   const long long Nf = grid_cells(p);
@@ -1699,6 +1705,7 @@ static void fill_info(const Plan<T>* p, cufinufft_plan_info* info) {
   info->es_c = p->sp.c;
   info->line_fft = p->line_fft ? 1 : 0;
   info->half_fft = p->half_fft ? 1 : 0;
+  info->fp64_df = p->fp64_df && p->method == 2 ? 1 : 0;  // the subproblem interpolation only
   info->cell_order = p->cell_order ? 1 : 0;
   info->width_rule = p->width_rule;
 }

@@ -39,7 +39,10 @@ constexpr int kMaxHornerRows = kMaxNS + 4;  // degree <= ns + 3
 // parameter block, so the unrolled evaluation reads them straight from the
 // constant bank.
 // FP64 plans also carry the fitted polynomials as FP32 pairs (hi + lo, the
-// double-float interpolation kernel evaluates them without FP64 units).
+// double-float interpolation kernel evaluates them without FP64 units),
+// scaled by 2^-E with E = round(beta log2 e) so that kernel values are ~1
+// (the kernel's peak e^beta, and the grid's 1/e^(d beta) scale, would leave
+// FP32's exponent range in 3D at wide kernels).
 template <typename T> struct DFCoef {};
 template <> struct DFCoef<double> {
   float hi[kMaxHornerRows * kMaxNS];
@@ -110,6 +113,7 @@ template <typename T> struct SpreadArgs {
   // next call on the plan reads; null: not recorded.
   int* status;
   int tma_wait_test;        // nonzero: every tile's first wait gives up at once (tests)
+  int fp64_df;              // FP64: subproblem interpolation in double-float (k_interp_sm_df)
 };
 
 // Cells of one subproblem tile: the bin plus the ns-1 cells its points

@@ -106,6 +106,7 @@ template <typename T> struct Plan {
   int* h_status = nullptr;
   int* d_status = nullptr;
   int tma_wait_test = 0;   // CUFINUFFT_TMA_WAIT_TEST=1 at makeplan
+  int fp64_df = 0;         // FP64 type 2: double-float subproblem interpolation
   // execute as a CUDA graph (timing off): captured for one pair of caller
   // arrays and one plan state (`version` counts setpts / set_layout)
   cudaGraph_t graph = nullptr;
@@ -220,8 +221,10 @@ inline SpreadArgs<T> spread_args(Plan<T>* p) {
   for (size_t k = 0; k < p->horner.size() && k < (size_t)(kMaxHornerRows * kMaxNS); ++k) {
     a.kc.coef[k] = p->horner[k];
     if constexpr (sizeof(T) == 8) {
-      a.kc.df.hi[k] = (float)p->horner[k];
-      a.kc.df.lo[k] = (float)(p->horner[k] - (double)a.kc.df.hi[k]);
+      // scaled by 2^-E, E = round(beta log2 e): kernel values ~1, see df_scale_exp
+      const double v = std::ldexp(p->horner[k], -(int)std::lround(p->sp.beta * 1.44269504088896340736));
+      a.kc.df.hi[k] = (float)v;
+      a.kc.df.lo[k] = (float)(v - (double)a.kc.df.hi[k]);
     }
   }
   a.g.Nf = grid_cells(p);
@@ -231,6 +234,7 @@ inline SpreadArgs<T> spread_args(Plan<T>* p) {
   a.sub_dense = a.run ? p->sub_dense : nullptr;
   a.status = p->d_status;
   a.tma_wait_test = p->tma_wait_test;
+  a.fp64_df = p->fp64_df;
   return a;
 }
 

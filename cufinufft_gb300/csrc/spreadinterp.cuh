@@ -582,7 +582,7 @@ k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) 
 }
 
 // ---------------------------------------------------------------------------
-// Double-float interpolation for FP64 plans (CUFINUFFT_FP64_DF=1).  GB300's
+// Double-float interpolation for FP64 plans (SpreadArgs::fp64_df).  GB300's
 // FP64 units are a small fraction of its FP32 throughput, and the FP64 tap
 // loop (2 FMAs per tap, ns^d taps) plus the FP64 kernel evaluation (a Horner
 // step per tap value and degree) bound FP64 interpolation.  Here the tile
@@ -609,7 +609,12 @@ struct DFAcc {
   __device__ __forceinline__ DF value() const { return df_renorm(s, t); }
 };
 
-// Kernel value phi(d - ns/2 + j) in double-float.
+// The kernel's power-of-two scale E = round(beta log2 e): kernel values are
+// taken times 2^-E and grid values times 2^(dim E), products unchanged
+// (exact scalings), every factor near 1 in FP32's exponent range.
+__device__ __forceinline__ int df_scale_exp(double beta) { return (int)rint(beta * 1.44269504088896340736); }
+
+// Kernel value phi(d - ns/2 + j) 2^-E in double-float.
 template <int NS, int HD>
 __device__ __forceinline__ DF df_kernel_tap(double d, int j, const KernelCoeffs<double>& kc) {
   if (kc.horner) {
@@ -627,7 +632,7 @@ __device__ __forceinline__ DF df_kernel_tap(double d, int j, const KernelCoeffs<
     return v;
   }
   const double x = d - 0.5 * NS + j;
-  return df_from(es_value(kc.c * x * x, kc.beta));
+  return df_from(ldexp(es_value(kc.c * x * x, kc.beta), -df_scale_exp(kc.beta)));
 }
 
 template <int DIM, int NS>
@@ -650,11 +655,13 @@ k_interp_sm_df(SpreadArgs<double> a, const __grid_constant__ CUtensorMap gmap, i
   if (!bulk) tile_load_periodic<double>(tile, src, st, a.g);
   if (bulk) tile_copy_wait<double>(tile, &tile_bar, src, st, a.g, a.status, a.tma_wait_test);
   __syncthreads();
-  // the tile in place as FP32 pairs: (re hi, re lo, im hi, im lo) per cell
+  // the tile in place as FP32 pairs: (re hi, re lo, im hi, im lo) per cell,
+  // scaled by 2^(DIM E) (exact)
   float4* tdf = reinterpret_cast<float4*>(tile);
+  const double gscale = ldexp(1.0, DIM * df_scale_exp(a.kc.beta));
   for (int i = threadIdx.x; i < st.ntile; i += blockDim.x) {
     const C v = tile[i];
-    const DF r = df_from(v.x), m = df_from(v.y);
+    const DF r = df_from(v.x * gscale), m = df_from(v.y * gscale);
     tdf[i] = make_float4(r.h, r.l, m.h, m.l);
   }
   __syncthreads();
@@ -710,10 +717,6 @@ k_interp_sm_df(SpreadArgs<double> a, const __grid_constant__ CUtensorMap gmap, i
   }
 }
 
-inline bool fp64_df_enabled() {
-  const char* v = std::getenv("CUFINUFFT_FP64_DF");
-  return v && v[0] == '1';
-}
 
 // ---------------------------------------------------------------------------
 // Warp-cooperative variants.  A warp works on PPW = 32 / L points at a time;
@@ -844,15 +847,16 @@ k_spread_gm_wc(SpreadArgs<T> a) {
 // other bank of 2 ns (interleaved complex), halving bank conflicts.
 template <typename T>
 __device__ __forceinline__ void plane_flush(const T* re, const T* im, cplx_t<T>* grid,
-                                            const SubTile& st, const GridGeom& g) {
+                                            const SubTile& st, const GridGeom& g, int pitch = 0) {
+  if (pitch == 0) pitch = st.TX;  // row pitch of the planes (elements)
   const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
   const int rows = st.TY * st.TZ;
   TileRows rw(threadIdx.x >> 5, st.TY);
   if (tile_in_grid(st, g)) {  // no wrap
     for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
       cplx_t<T>* dst = grid + ((size_t)(st.oz + rw.iz) * g.nf[1] + st.oy + rw.iy) * g.nf[0] + st.ox;
-      const T* rr = re + r * st.TX;
-      const T* ri = im + r * st.TX;
+      const T* rr = re + r * pitch;
+      const T* ri = im + r * pitch;
       for (int ix = lane; ix < st.TX; ix += 32) {
         const T vr = rr[ix], vi = ri[ix];
         if (vr == T(0) && vi == T(0)) continue;
@@ -865,7 +869,7 @@ __device__ __forceinline__ void plane_flush(const T* re, const T* im, cplx_t<T>*
     const int gy = wrap3(st.oy + rw.iy, g.nf[1]), gz = wrap3(st.oz + rw.iz, g.nf[2]);
     cplx_t<T>* dst = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
     for (int ix = lane; ix < st.TX; ix += 32) {
-      const T vr = re[r * st.TX + ix], vi = im[r * st.TX + ix];
+      const T vr = re[r * pitch + ix], vi = im[r * pitch + ix];
       if (vr == T(0) && vi == T(0)) continue;
       red_add(dst + wrap3(st.ox + ix, g.nf[0]), vr, vi);
     }
@@ -924,6 +928,115 @@ k_spread_sm_wc(SpreadArgs<T> a) {
   }
   __syncthreads();
   plane_flush<T>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g);
+}
+
+// ---------------------------------------------------------------------------
+// Slab-owned 3D spreading (method 2, the default for sparse 3D subproblems).
+// Shared FP32 atomicAdd runs at about a third of the int32 rate and costs
+// several shared wavefronts per warp instruction, which bound the
+// warp-cooperative kernel.  Here the tile's z-planes are owned: the block has
+// NS warps and warp w alone writes the planes z = w (mod NS).  A point's
+// support covers NS consecutive planes, one of each residue, so every warp
+// handles exactly one plane of every point, and it adds the point's NS x NS
+// taps there with plain shared loads and stores: lanes over (x, y) taps, R =
+// 32 / NS rows per instruction, distinct cells, and a __syncwarp between
+// points, which orders one point's stores before the next point's loads.
+// The block stages the kernel values of CH points at a time (c kx as
+// complex, ky, kz, the point's tile offset) in a double buffer, one block
+// barrier per chunk.  Rows are padded to a pitch PX = -NS (mod 32), so the R
+// rows of an instruction fall in disjoint banks.  Results equal the atomic
+// kernels' up to the order of additions.
+constexpr int kSlabChunk = 64;
+
+__host__ __device__ constexpr int slab_pitch(int tx, int ns) {
+  return tx + (((32 - ns - tx) % 32) + 32) % 32;
+}
+
+template <typename T>
+size_t slab_bytes(int ns, const BinTables& bt) {
+  const size_t px = slab_pitch(bt.bs[0] + ns - 1, ns);
+  const size_t cells = px * (bt.bs[1] + ns - 1) * (bt.bs[2] + ns - 1);
+  const size_t stage = (size_t)kSlabChunk * ns * (sizeof(cplx_t<T>) + 2 * sizeof(T)) + kSlabChunk * 2 * sizeof(int);
+  return cells * 2 * sizeof(T) + 16 + 2 * stage;  // stage aligned to 16 bytes
+}
+
+template <typename T, int NS>
+__global__ void __launch_bounds__(32 * NS)
+k_spread_sm_slab(SpreadArgs<T> a) {
+  using C = cplx_t<T>;
+  constexpr int HD = horner_degree<T>(NS);
+  constexpr int R = 32 / NS;                 // tile rows per warp instruction
+  constexpr int NR = (NS + R - 1) / R;       // instructions per plane
+  constexpr int CH = kSlabChunk;
+  if (a.sub_dense && a.sub_dense[blockIdx.x]) return;  // cell-run layout: done by k_spread_sm_run
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const SubTile st = sub_tile_block<3, NS>(a.bins, blockIdx.x);
+  const int PX = slab_pitch(st.TX, NS);
+  const int PP = PX * st.TY;                  // plane stride
+  const int ncell = PP * st.TZ;
+  T* re = reinterpret_cast<T*>(smem_raw);
+  T* im = re + ncell;
+  // double-buffered stage: [c kx (complex) | ky | kz] x CH x NS, then base, lz
+  unsigned char* stage0 = smem_raw + ((2 * (size_t)ncell * sizeof(T) + 15) & ~(size_t)15);
+  const size_t stage_sz = (size_t)CH * NS * (sizeof(C) + 2 * sizeof(T)) + CH * 2 * sizeof(int);
+  const int t = blockIdx.y;
+  for (int i = threadIdx.x; i < 2 * ncell; i += blockDim.x) re[i] = T(0);
+  const C* cin = a.c_in + (size_t)t * a.M;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int dx = lane % NS, dyl = lane / NS;
+  const bool lane_on = lane < R * NS;
+  for (int c0 = 0, buf = 0; c0 < st.np; c0 += CH, buf ^= 1) {
+    unsigned char* sb = stage0 + buf * stage_sz;
+    C* s_ck = reinterpret_cast<C*>(sb);
+    T* s_ky = reinterpret_cast<T*>(s_ck + CH * NS);
+    T* s_kz = s_ky + CH * NS;
+    int* s_base = reinterpret_cast<int*>(s_kz + CH * NS);
+    int* s_lz = s_base + CH;
+    const int nq = min(CH, st.np - c0);
+    for (int i = threadIdx.x; i < nq * NS; i += blockDim.x) {
+      const int q = i / NS, j = i - q * NS;
+      const int p = st.p0 + c0 + q;
+      const C v = cin[a.pts.idx[p]];
+      const T kx = kernel_tap<T, NS, HD>(a.pts.d[0][p], j, a.kc);
+      s_ck[i] = C{v.x * kx, v.y * kx};
+      s_ky[i] = kernel_tap<T, NS, HD>(a.pts.d[1][p], j, a.kc);
+      s_kz[i] = kernel_tap<T, NS, HD>(a.pts.d[2][p], j, a.kc);
+      if (j == 0) {
+        const int lx = a.pts.i0[0][p] - st.ox, ly = a.pts.i0[1][p] - st.oy, lz = a.pts.i0[2][p] - st.oz;
+        s_base[q] = (lz * st.TY + ly) * PX + lx;
+        s_lz[q] = lz;
+      }
+    }
+    __syncthreads();  // (also: the tile is zeroed; the other buffer is free)
+    for (int q = 0; q < nq; ++q) {
+      int dz = (warp - s_lz[q]) % NS;
+      dz += dz < 0 ? NS : 0;                  // the plane of residue `warp`
+      const T kz = s_kz[q * NS + dz];
+      const C ck = s_ck[q * NS + dx];
+      const T ur = ck.x * kz, ui = ck.y * kz;
+      const int base = s_base[q] + dz * PP + dx;
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const int dy = r * R + dyl;
+        if (lane_on && dy < NS) {
+          const T ky = s_ky[q * NS + dy];
+          const int o = base + dy * PX;
+          re[o] = fma_rn(ur, ky, re[o]);
+          im[o] = fma_rn(ui, ky, im[o]);
+        }
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  plane_flush<T>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g, PX);
+}
+
+// CUFINUFFT_SPREAD_SLAB=0: 3D subproblem spreading by the warp-cooperative
+// atomic kernel instead of the slab-owned one.
+inline bool slab_spread_enabled() {
+  const char* v = std::getenv("CUFINUFFT_SPREAD_SLAB");
+  return !(v && v[0] == '0');
 }
 
 // ---------------------------------------------------------------------------
@@ -1432,14 +1545,40 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
     }
   } else {
     if (a.bins.nsub == 0) return cudaSuccess;
+    // 3D sparse subproblems: the slab-owned kernel unless a variant is forced
+    bool slab = false;
+    if constexpr (DIM == 3) {
+      slab = a.variant == 0 && slab_spread_enabled();
+      if (slab) {  // its padded tile and staging must fit (else the atomic kernel)
+        int dev = 0, optin = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e != cudaSuccess) return e;
+        slab = slab_bytes<T>(NS, a.bins) <= (size_t)optin;
+      }
+    }
+    auto sparse = [&]() -> cudaError_t {
+      if constexpr (DIM == 3) {
+        if (slab) {
+          const size_t smb = slab_bytes<T>(NS, a.bins);
+          cudaError_t e = prepare_smem(k_spread_sm_slab<T, NS>, smb);
+          if (e != cudaSuccess) return e;
+          k_spread_sm_slab<T, NS><<<dim3(a.bins.nsub, a.ntr), 32 * NS, smb, s>>>(a);
+          return cudaGetLastError();
+        }
+      }
+      const size_t smw = tile_bytes<T, DIM>(NS, a.bins);
+      cudaError_t e = prepare_smem(k_spread_sm_wc<T, DIM, NS>, smw);
+      if (e != cudaSuccess) return e;
+      k_spread_sm_wc<T, DIM, NS><<<dim3(a.bins.nsub, a.ntr), kSpreadThreads, smw, s>>>(a);
+      return cudaGetLastError();
+    };
     if constexpr (run_ok<DIM, NS>()) {
       if (a.run) {
         // subproblems starting on a dense cell take the cell-run kernel, the
-        // others the warp-cooperative one (each kernel skips the other kind)
-        const size_t smw = tile_bytes<T, DIM>(NS, a.bins);
-        cudaError_t e = prepare_smem(k_spread_sm_wc<T, DIM, NS>, smw);
+        // others the sparse kernel (each kernel skips the other kind)
+        cudaError_t e = sparse();
         if (e != cudaSuccess) return e;
-        k_spread_sm_wc<T, DIM, NS><<<dim3(a.bins.nsub, a.ntr), kSpreadThreads, smw, s>>>(a);
         if constexpr (sizeof(T) == 4 && DIM == 3 && NS <= 8) {
           if (tc_spread_enabled()) {
             const size_t smt = tc_run_bytes(NS, a.bins);
@@ -1457,6 +1596,7 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
       }
     }
     if (a.run) return cudaErrorInvalidValue;  // more than 512 taps per point
+    if (slab) return sparse();
     size_t sm = tile_bytes<T, DIM>(NS, a.bins);
     cudaError_t e = wc ? prepare_smem(k_spread_sm_wc<T, DIM, NS>, sm)
                        : prepare_smem(k_spread_sm<T, DIM, NS>, sm);
@@ -1502,7 +1642,7 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
       }
     }
     if constexpr (sizeof(T) == 8) {
-      if (!wc && fp64_df_enabled()) {
+      if (!wc && a.fp64_df) {
         cudaError_t e = prepare_smem(k_interp_sm_df<DIM, NS>, sm);
         if (e != cudaSuccess) return e;
         k_interp_sm_df<DIM, NS><<<dim3(a.bins.nsub, a.ntr), kInterpThreads, sm, s>>>(a, gmap, tma);

@@ -36,7 +36,7 @@
 /* Return codes.  1..9 are the reference's (contrib/utils.h:28-36 and the
  * method checks in src/2d/spread2d_wrapper.cu:155); 10.. are this library's. */
 #define CUFINUFFT_WARN_EPS_TOO_SMALL 1
-#define CUFINUFFT_ERR_GENERIC 1        /* also: type 3, bad binsize, NULL plan */
+#define CUFINUFFT_ERR_GENERIC 1        /* also: bad type, bad binsize, NULL plan */
 #define CUFINUFFT_ERR_METHOD 2         /* gpu_method not valid for this dim/type */
 #define CUFINUFFT_ERR_UPSAMPFAC_TOO_SMALL 7
 #define CUFINUFFT_ERR_HORNER_WRONG_BETA 8
@@ -112,6 +112,7 @@ typedef struct cufinufft_plan_info {
   int width_rule; /* kernel-width rule the plan was made under (cufinufft_set_width_rule) */
   int chain_fp32; /* 1: an FP64 plan running its spread/interp, FFT and deconvolution in FP32 */
   int half_fft;   /* 1: pruned power-of-two FFT passes (halffft.cu) instead of cuFFT */
+  int fp64_df;    /* 1: an FP64 type-2 method-2 plan interpolating in double-float (FP32 pairs) */
 } cufinufft_plan_info;
 int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info);
 int cufinufftf_get_info(cufinufftf_plan plan, cufinufft_plan_info* info);
@@ -249,6 +250,15 @@ int cufinufftf_batch_destroy(cufinufftf_batch batch);
 int cufinufftf_spread2d_noalloc(int M, const float* x, const float* y, const cuFloatComplex* c,
                                 int nf1, int nf2, float tol, cuFloatComplex* fw,
                                 cudaStream_t stream);
+
+/* Measured accumulation ceilings of the current device (no counterpart in
+ * the reference): lane operations per second of kind 0 = shared-memory FP32
+ * atomicAdd, 1 = shared-memory int32 atomicAdd, 2 = global 8-byte
+ * red.global.add.v2.f32 into L2-resident addresses, 3 = shared-memory 64-bit
+ * integer atomicAdd, every lane of a warp on its own address.  The spread kernels are bound by these rather than by
+ * HBM; the benchmark's type-1 roofline divides by them.  Allocates, runs
+ * two short launches on a private stream and synchronises it. */
+int cufinufft_atomic_rate(int kind, double* lane_ops_per_s);
 
 #ifdef __cplusplus
 }

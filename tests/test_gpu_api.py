@@ -304,3 +304,17 @@ def test_type2_padding_stays_zero_across_executes():
             assert err < (2e-5 if single else 1e-10), (single, rep, err)
             if rep == 0:
                 plan.autotune()
+
+
+def test_atomic_rate_probe():
+    """The accumulation ceilings the type-1 roofline divides by: positive,
+    finite, and bad kinds / NULL outputs refused."""
+    from cufinufft_gb300 import _cufinufft as cl
+    for kind in (0, 1, 2, 3):
+        r = ctypes.c_double(0.0)
+        assert cl.atomic_rate(kind, ctypes.byref(r)) == 0
+        # between 1e10 and 1e15 lane operations per second on any recent GPU
+        assert 1e10 < r.value < 1e15, (kind, r.value)
+    r = ctypes.c_double(0.0)
+    assert cl.atomic_rate(4, ctypes.byref(r)) == 13
+    assert cl.atomic_rate(0, None) == 13
