@@ -183,7 +183,9 @@ template <typename T> static void release(Plan<T>* p) {
   p->sparse_count = nullptr;
   p->cap_sparse = 0;
   cudaFree(p->sub_dense);
+  cudaFree(p->sub_ndense);
   p->sub_dense = nullptr;
+  p->sub_ndense = nullptr;
   p->cap_sub_dense = 0;
   if (p->h_total) cudaFreeHost(p->h_total);
   p->h_total = nullptr;
@@ -1756,9 +1758,12 @@ static int build_subproblems(Plan<T>* p) {
   if (p->cell_order) {
     if ((size_t)nsub > p->cap_sub_dense) {
       cudaFree(p->sub_dense);
+      cudaFree(p->sub_ndense);
       p->sub_dense = nullptr;
+      p->sub_ndense = nullptr;
       p->cap_sub_dense = 0;
       CFG_CUDA(cudaMalloc(&p->sub_dense, (size_t)nsub));
+      CFG_CUDA(cudaMalloc(&p->sub_ndense, sizeof(int) * (size_t)nsub));
       p->cap_sub_dense = nsub;
     }
     SubClassArgs c;
@@ -1778,6 +1783,9 @@ static int build_subproblems(Plan<T>* p) {
     c.nsub = nsub;
     c.dense_min = dense_run(p->dim);
     c.dense = p->sub_dense;
+    c.cls_start = p->cls_start;
+    c.count = p->count;
+    c.ndense = p->sub_ndense;
     CFG_CUDA(launch_classify_subproblems(c, p->stream));
   }
   return 0;

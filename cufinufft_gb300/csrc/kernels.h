@@ -122,6 +122,11 @@ struct SubClassArgs {
   int bs[3];
   int dim, maxsub, ncls, nsub, dense_min;
   unsigned char* dense;
+  // optional: per subproblem, its leading points on dense cells (a bin's
+  // dense cells come first), from the scanned dense counts and bin counts
+  const int* cls_start;
+  const int* count;
+  int* ndense;
 };
 cudaError_t launch_classify_subproblems(const SubClassArgs& a, cudaStream_t s);
 // The driver's cuTensorMapEncodeTiled, looked up once per process (null if

@@ -107,6 +107,7 @@ template <typename T> struct SpreadArgs {
   int variant;              // kernel family: 0 default, 1 one thread per point, 2 warp-cooperative
   int run;                  // method 2 spreading over cell-ordered points (cell-run kernel)
   const unsigned char* sub_dense;  // run: subproblems that start on a dense cell
+  const int* sub_ndense;           // run: leading points on dense cells per subproblem
   // Interpolation tile waits (bulk copies): status[0] is set when a wait ran
   // out and the tile was loaded cell by cell instead, status[1] when the copy
   // had still not landed after a second full wait.  Host-mapped memory the

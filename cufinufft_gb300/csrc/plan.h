@@ -74,6 +74,7 @@ template <typename T> struct Plan {
   size_t cap_sparse = 0;
   unsigned char* sub_dense = nullptr;  // per subproblem: starts on a dense cell (cell order)
   size_t cap_sub_dense = 0;
+  int* sub_ndense = nullptr;  // cell order: leading dense points per subproblem
   // FP64 plans whose tolerance allows it run the spread/interp, FFT and
   // deconvolution chain in FP32: `lo` is that FP32 plan (null otherwise).
   // This side folds and rescales the points in FP64 (n_* arrays: caller
@@ -232,6 +233,7 @@ inline SpreadArgs<T> spread_args(Plan<T>* p) {
   a.variant = p->variant;
   a.run = (p->cell_order && p->type == 1 && p->method == 2) ? 1 : 0;
   a.sub_dense = a.run ? p->sub_dense : nullptr;
+  a.sub_ndense = a.run ? p->sub_ndense : nullptr;
   a.status = p->d_status;
   a.tma_wait_test = p->tma_wait_test;
   a.fp64_df = p->fp64_df;

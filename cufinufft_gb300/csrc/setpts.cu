@@ -453,6 +453,12 @@ __global__ void k_classify_subproblems(SubClassArgs a) {
     const int lz = a.dim > 2 ? a.i0[2][p0] % a.bs[2] : 0;
     const int c = lx + a.bs[0] * (ly + a.bs[1] * lz);
     a.dense[sidx] = a.cls_count[(long long)b * a.ncls + c] >= a.dense_min ? 1 : 0;
+    if (a.ndense) {
+      const int js = sidx - a.sub_start[b];
+      const int np = min(a.maxsub, a.count[b] - js * a.maxsub);
+      const int nd = a.cls_start[(long long)(b + 1) * a.ncls] - a.cls_start[(long long)b * a.ncls];
+      a.ndense[sidx] = max(0, min(np, nd - js * a.maxsub));
+    }
   }
 }
 

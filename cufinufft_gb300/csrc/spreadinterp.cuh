@@ -956,42 +956,49 @@ template <typename T>
 size_t slab_bytes(int ns, const BinTables& bt) {
   const size_t px = slab_pitch(bt.bs[0] + ns - 1, ns);
   const size_t cells = px * (bt.bs[1] + ns - 1) * (bt.bs[2] + ns - 1);
-  const size_t stage = (size_t)kSlabChunk * ns * (sizeof(cplx_t<T>) + 2 * sizeof(T)) + kSlabChunk * 2 * sizeof(int);
+  const size_t stage = (size_t)kSlabChunk * ns * (sizeof(cplx_t<T>) + 2 * sizeof(T)) + kSlabChunk * sizeof(int2);
   return cells * 2 * sizeof(T) + 16 + 2 * stage;  // stage aligned to 16 bytes
 }
 
 template <typename T, int NS>
 __global__ void __launch_bounds__(32 * NS)
-k_spread_sm_slab(SpreadArgs<T> a) {
+k_spread_sm_slab(SpreadArgs<T> a, int split) {
   using C = cplx_t<T>;
   constexpr int HD = horner_degree<T>(NS);
   constexpr int R = 32 / NS;                 // tile rows per warp instruction
   constexpr int NR = (NS + R - 1) / R;       // instructions per plane
   constexpr int CH = kSlabChunk;
-  if (a.sub_dense && a.sub_dense[blockIdx.x]) return;  // cell-run layout: done by k_spread_sm_run
+  // cell-run layout: a subproblem that starts on a dense cell leaves its
+  // leading dense points to k_spread_sm_run (split) or all of them (not)
+  int first = 0;
+  if (a.sub_dense && a.sub_dense[blockIdx.x]) {
+    if (!split) return;
+    first = a.sub_ndense[blockIdx.x];
+  }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const SubTile st = sub_tile_block<3, NS>(a.bins, blockIdx.x);
+  if (first >= st.np) return;  // block-uniform
   const int PX = slab_pitch(st.TX, NS);
   const int PP = PX * st.TY;                  // plane stride
   const int ncell = PP * st.TZ;
   T* re = reinterpret_cast<T*>(smem_raw);
   T* im = re + ncell;
-  // double-buffered stage: [c kx (complex) | ky | kz] x CH x NS, then base, lz
+  // double-buffered stage: [c kx (complex) | ky | kz] x CH x NS, then
+  // (tile offset, lz mod NS) per point
   unsigned char* stage0 = smem_raw + ((2 * (size_t)ncell * sizeof(T) + 15) & ~(size_t)15);
-  const size_t stage_sz = (size_t)CH * NS * (sizeof(C) + 2 * sizeof(T)) + CH * 2 * sizeof(int);
+  const size_t stage_sz = (size_t)CH * NS * (sizeof(C) + 2 * sizeof(T)) + CH * sizeof(int2);
   const int t = blockIdx.y;
   for (int i = threadIdx.x; i < 2 * ncell; i += blockDim.x) re[i] = T(0);
   const C* cin = a.c_in + (size_t)t * a.M;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int dx = lane % NS, dyl = lane / NS;
   const bool lane_on = lane < R * NS;
-  for (int c0 = 0, buf = 0; c0 < st.np; c0 += CH, buf ^= 1) {
+  for (int c0 = first, buf = 0; c0 < st.np; c0 += CH, buf ^= 1) {
     unsigned char* sb = stage0 + buf * stage_sz;
     C* s_ck = reinterpret_cast<C*>(sb);
     T* s_ky = reinterpret_cast<T*>(s_ck + CH * NS);
     T* s_kz = s_ky + CH * NS;
-    int* s_base = reinterpret_cast<int*>(s_kz + CH * NS);
-    int* s_lz = s_base + CH;
+    int2* s_bl = reinterpret_cast<int2*>(s_kz + CH * NS);
     const int nq = min(CH, st.np - c0);
     for (int i = threadIdx.x; i < nq * NS; i += blockDim.x) {
       const int q = i / NS, j = i - q * NS;
@@ -1003,18 +1010,18 @@ k_spread_sm_slab(SpreadArgs<T> a) {
       s_kz[i] = kernel_tap<T, NS, HD>(a.pts.d[2][p], j, a.kc);
       if (j == 0) {
         const int lx = a.pts.i0[0][p] - st.ox, ly = a.pts.i0[1][p] - st.oy, lz = a.pts.i0[2][p] - st.oz;
-        s_base[q] = (lz * st.TY + ly) * PX + lx;
-        s_lz[q] = lz;
+        s_bl[q] = make_int2((lz * st.TY + ly) * PX + lx, lz % NS);
       }
     }
     __syncthreads();  // (also: the tile is zeroed; the other buffer is free)
     for (int q = 0; q < nq; ++q) {
-      int dz = (warp - s_lz[q]) % NS;
+      const int2 bl = s_bl[q];
+      int dz = warp - bl.y;
       dz += dz < 0 ? NS : 0;                  // the plane of residue `warp`
       const T kz = s_kz[q * NS + dz];
       const C ck = s_ck[q * NS + dx];
       const T ur = ck.x * kz, ui = ck.y * kz;
-      const int base = s_base[q] + dz * PP + dx;
+      const int base = bl.x + dz * PP + dx;
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
         const int dy = r * R + dyl;
@@ -1025,7 +1032,7 @@ k_spread_sm_slab(SpreadArgs<T> a) {
           im[o] = fma_rn(ui, ky, im[o]);
         }
       }
-      __syncwarp();
+      __syncwarp();  // this point's stores before the next point's loads
     }
   }
   __syncthreads();
@@ -1063,7 +1070,8 @@ template <int DIM, int NS> constexpr bool run_ok() { return run_taps<DIM, NS>() 
 // point's NS kernel values along one axis, ktap(d, j) returns one of them.
 template <typename T, int DIM, int NS, class KRow, class KTap>
 __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, const SortedPts<T>& pts,
-                                               const cplx_t<T>* cin, KRow krow, KTap ktap) {
+                                               const cplx_t<T>* cin, KRow krow, KTap ktap,
+                                               bool prefix_only = false) {
   using C = cplx_t<T>;
   constexpr int NT = run_taps<DIM, NS>();
   constexpr int KV = DIM * NS;
@@ -1086,8 +1094,12 @@ __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, 
   // (points on the window's first cell) has at least dense_run(DIM) points is
   // accumulated -- the run's first n <= 32 points -- and the cursor moves by
   // n, so the next window starts at a run boundary; any other window is
-  // spread point by point and the cursor moves by 32.
-  constexpr int kMinRun = dense_run(DIM);
+  // spread point by point and the cursor moves by 32.  prefix_only: the
+  // points are a subproblem's dense prefix (every cell holds a run), so a
+  // leading run of at least 4 points is accumulated too, and a shorter one
+  // (a run's remainder) is spread point by point alone: the cursor never
+  // leaves a run boundary.
+  const int kMinRun = prefix_only ? 4 : dense_run(DIM);
   int cs = beg;
   while (cs < end) {  // warp-uniform
     const int ql = cs + lane;
@@ -1120,6 +1132,55 @@ __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, 
       }
       cvw[lane] = cin[pts.idx[p]];
       __syncwarp();
+      if constexpr (DIM == 3 && NS >= 5) {
+        // factorised: lane (ix, iy0) owns the taps (ix, iy0 + m R3, iz) for
+        // all iz; per point it reads c, kx[ix], its ky values and the ns kz
+        // values (broadcast), and adds (c kx ky) kz to NR3 x NS sums
+        constexpr int R3 = 32 / NS, NR3 = (NS + R3 - 1) / R3;
+        const int fx = lane % NS, fy = lane / NS;
+        T accr[NR3][NS], acci[NR3][NS];
+#pragma unroll
+        for (int m = 0; m < NR3; ++m)
+#pragma unroll
+          for (int iz = 0; iz < NS; ++iz) accr[m][iz] = acci[m][iz] = T(0);
+#pragma unroll 2
+        for (int q = 0; q < nrun; ++q) {
+          const T* kq = kvw + q * KV;
+          const C cq = cvw[q];
+          const T kxv = kq[fx];
+          const T cr = cq.x * kxv, ci = cq.y * kxv;
+          T kzv[NS];
+#pragma unroll
+          for (int iz = 0; iz < NS; ++iz) kzv[iz] = kq[2 * NS + iz];
+#pragma unroll
+          for (int m = 0; m < NR3; ++m) {
+            const T kyv = kq[NS + min(fy + m * R3, NS - 1)];
+            const T wr = cr * kyv, wi = ci * kyv;
+#pragma unroll
+            for (int iz = 0; iz < NS; ++iz) {
+              accr[m][iz] = fma_rn(wr, kzv[iz], accr[m][iz]);
+              acci[m][iz] = fma_rn(wi, kzv[iz], acci[m][iz]);
+            }
+          }
+        }
+        if (lane < R3 * NS) {
+#pragma unroll
+          for (int m = 0; m < NR3; ++m) {
+            const int iy = fy + m * R3;
+            if (iy < NS) {
+#pragma unroll
+              for (int iz = 0; iz < NS; ++iz) {
+                const int off = key0 + fx + st.TX * (iy + st.TY * iz);
+                atomicAdd(re + off, accr[m][iz]);
+                atomicAdd(im + off, acci[m][iz]);
+              }
+            }
+          }
+        }
+        __syncwarp();  // the staging area is rewritten by the next chunk
+        cs += nrun;
+        continue;
+      }
 #pragma unroll 1
       for (int pass = 0; pass < NPASS; ++pass) {
         int ix[GK], iy[GK], iz[GK];
@@ -1163,12 +1224,13 @@ __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, 
       const int g = lane / L, j = lane % L;
       const bool tap = j < NS;
       const int jj = tap ? j : 0;
+      const int lim = prefix_only ? nrun : 32;  // points of this window
       // cell-ordered neighbours overlap: group g takes points it + g * NIT,
       // so the PPW points of one warp instruction lie far apart in the chunk
-      constexpr int NIT = (32 + PPW - 1) / PPW;
+      const int NIT = (lim + PPW - 1) / PPW;
       for (int it = 0; it < NIT; ++it) {  // warp-uniform
         const int qq = it + g * NIT;
-        const bool v2 = g < PPW && qq < 32 && cs + qq < end;
+        const bool v2 = g < PPW && qq < lim && cs + qq < end;
         const int p2 = st.p0 + (v2 ? cs + qq : cs);
         const int lx2 = pts.i0[0][p2] - st.ox;
         const T kx = ktap(pts.d[0][p2], jj);
@@ -1194,18 +1256,19 @@ __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, 
           }
         }
       }
-      cs += 32;
+      cs += lim;
     }
   }
 }
 
 template <typename T, int DIM, int NS>
 __global__ void __launch_bounds__(kSpreadThreads)
-k_spread_sm_run(SpreadArgs<T> a) {
+k_spread_sm_run(SpreadArgs<T> a, int split) {
   constexpr int HD = horner_degree<T>(NS);
-  if (a.sub_dense && !a.sub_dense[blockIdx.x]) return;  // sparse: done by k_spread_sm_wc
+  if (a.sub_dense && !a.sub_dense[blockIdx.x]) return;  // sparse: done by k_spread_sm_wc / slab
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
+  SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
+  if (split) st.np = a.sub_ndense[blockIdx.x];  // the rest: k_spread_sm_slab
   T* re = reinterpret_cast<T*>(smem_raw);
   T* im = re + st.ntile;
   const int t = blockIdx.y;
@@ -1215,7 +1278,7 @@ k_spread_sm_run(SpreadArgs<T> a) {
   run_subproblem<T, DIM, NS>(
       st, re, im, a.pts, a.c_in + (size_t)t * a.M,
       [&](T dv, T* out) { kernel_row<T, NS, HD>(dv, kc, out); },
-      [&](T dv, int j) { return kernel_tap<T, NS, HD>(dv, j, kc); });
+      [&](T dv, int j) { return kernel_tap<T, NS, HD>(dv, j, kc); }, split != 0);
   __syncthreads();
   plane_flush<T>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g);
 }
@@ -1546,7 +1609,7 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
   } else {
     if (a.bins.nsub == 0) return cudaSuccess;
     // 3D sparse subproblems: the slab-owned kernel unless a variant is forced
-    bool slab = false;
+    bool slab = false, split = false;
     if constexpr (DIM == 3) {
       slab = a.variant == 0 && slab_spread_enabled();
       if (slab) {  // its padded tile and staging must fit (else the atomic kernel)
@@ -1556,6 +1619,11 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
         if (e != cudaSuccess) return e;
         slab = slab_bytes<T>(NS, a.bins) <= (size_t)optin;
       }
+      // cell-run layout: the slab kernel also takes the sparse tails of the
+      // dense subproblems (the tensor-core form walks whole subproblems)
+      bool tc = false;
+      if constexpr (sizeof(T) == 4 && NS <= 8) tc = tc_spread_enabled();
+      split = slab && a.run && a.sub_ndense != nullptr && !tc;
     }
     auto sparse = [&]() -> cudaError_t {
       if constexpr (DIM == 3) {
@@ -1563,7 +1631,7 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
           const size_t smb = slab_bytes<T>(NS, a.bins);
           cudaError_t e = prepare_smem(k_spread_sm_slab<T, NS>, smb);
           if (e != cudaSuccess) return e;
-          k_spread_sm_slab<T, NS><<<dim3(a.bins.nsub, a.ntr), 32 * NS, smb, s>>>(a);
+          k_spread_sm_slab<T, NS><<<dim3(a.bins.nsub, a.ntr), 32 * NS, smb, s>>>(a, split ? 1 : 0);
           return cudaGetLastError();
         }
       }
@@ -1591,7 +1659,7 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
         const size_t sm = run_bytes<T, DIM>(NS, a.bins);
         e = prepare_smem(k_spread_sm_run<T, DIM, NS>, sm);
         if (e != cudaSuccess) return e;
-        k_spread_sm_run<T, DIM, NS><<<dim3(a.bins.nsub, a.ntr), kSpreadThreads, sm, s>>>(a);
+        k_spread_sm_run<T, DIM, NS><<<dim3(a.bins.nsub, a.ntr), kSpreadThreads, sm, s>>>(a, split ? 1 : 0);
         return cudaGetLastError();
       }
     }

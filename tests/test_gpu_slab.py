@@ -66,7 +66,9 @@ def _run_cellrun(pts, c, modes, tol):
     return fk.cpu().numpy(), info
 
 
-def test_slab_spread_cellrun_sparse_part(monkeypatch):
+def test_slab_spread_cellrun_layout(monkeypatch):
+    """Cell-run layout: the slab kernel takes the sparse subproblems and the
+    cell-run kernel the dense ones."""
     rng = np.random.default_rng(17)
     M, modes = 40000, (32, 30, 28)
     half = M // 2
@@ -79,7 +81,7 @@ def test_slab_spread_cellrun_sparse_part(monkeypatch):
     ref_wc, _ = _run_cellrun(pts, c, modes, 1e-5)
     monkeypatch.delenv("CUFINUFFT_SPREAD_SLAB")
     out, info = _run_cellrun(pts, c, modes, 1e-5)
-    assert _rel(out, ref_wc) < 1e-6, info
+    assert _rel(out, ref_wc) < 5e-6, info   # dense cells: long FP32 sums in another order
     ref = NC.oracle_nufft(1, modes, [p.astype(np.float64) for p in pts], c, 1e-5, True,
                           gpu_method=2)
     assert _rel(out, ref) < 2e-5, info
