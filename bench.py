@@ -25,7 +25,9 @@ the timed events); `e2e` times the same public call with the input copied
 from pinned host memory and the output copied back inside each step.
 
 --impl reference times the CPU restatement of the reference's algorithm
-(oracle/, FP64 arithmetic, all host cores, scipy FFT) on the same workload.
+(oracle/, in the workload's precision -- FP32 arithmetic for FP32 workloads,
+as the reference's FP32 build computes -- all host cores, scipy FFT) on the
+same workload.
 
 Multi-GPU: replicas -- each rank runs the workload on its own GPU; no data
 moves between ranks; value = sum of points / max time over ranks.
@@ -276,11 +278,16 @@ def atomic_roofline(taps: int, k_ms: float, single: bool) -> dict:
                     "cufinufft_atomic_rate; FP64 plans: no FP32 peak applies"}
 
 
-def oracle_plan(w: Workload, cores: int, ns=None):
+def oracle_plan(w: Workload, cores: int, ns=None, timing=False):
+    """The oracle's plan for this workload.  timing: the CPU legs (baseline
+    and reference arm) run in the workload's own precision -- FP32 arithmetic
+    for FP32 workloads, as the reference's FP32 build computes -- while the
+    accuracy check stays FP64."""
     from oracle import oracle as O
     O.set_num_threads(cores)
     plan = O.OraclePlan(w.ntype, w.modes, 1 if w.ntype == 1 else -1, w.tol, w.single, ns=ns,
-                        upsampfac=w.upsampfac if ns is not None else 2.0)
+                        upsampfac=w.upsampfac if ns is not None else 2.0,
+                        fp32_arith=timing and w.single)
     plan.fft_workers = cores
     return plan
 
@@ -294,7 +301,7 @@ def cpu_sample(w: Workload, budget_s=20.0):
     """Bounded CPU sample of the workload: full execs while one fits the
     budget, else a subset of the points (spread/interp scale with M)."""
     cores = os.cpu_count() or 1
-    plan = oracle_plan(w, cores)
+    plan = oracle_plan(w, cores, timing=True)
     pts = [p.astype(np.float64) for p in w.points()]
     data = w.data().astype(np.complex128)
     M = pts[0].size
@@ -315,7 +322,8 @@ def cpu_sample(w: Workload, budget_s=20.0):
         cpu_step(plan, w, pts, data)
     dt = (time.perf_counter() - t0) / reps
     sample = (f"{reps} execs of {'the full workload' if frac == 1.0 else f'{Ms} of {M} points'}"
-              f" ({dt:.3f} s each), FP64 oracle restatement of the reference's path, scipy FFT")
+              f" ({dt:.3f} s each), oracle restatement of the reference's path in "
+              f"{'FP32' if w.single else 'FP64'} arithmetic, scipy FFT")
     return Ms * w.ntransf / dt, cores, sample
 
 
@@ -373,7 +381,7 @@ def run_reference(args, w: Workload, rank, world):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    plan = oracle_plan(w, cores)
+    plan = oracle_plan(w, cores, timing=True)
     pts = [p.astype(np.float64) for p in w.points()]
     data = w.data().astype(np.complex128)
     M = pts[0].size
@@ -401,11 +409,13 @@ def run_reference(args, w: Workload, rank, world):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if w.single else "f64",
         "data": "synthetic (seeded)",
         "config": {"workload": w.desc, "global_batch": 1, "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": sample + "; FP64 oracle restatement of the reference's path "
+                         "sample": sample + f"; oracle restatement of the reference's path in "
+                                            f"{'FP32' if w.single else 'FP64'} arithmetic "
                                             "(spread/interp + deconvolve in C/OpenMP, scipy FFT)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

@@ -1071,7 +1071,7 @@ template <int DIM, int NS> constexpr bool run_ok() { return run_taps<DIM, NS>() 
 template <typename T, int DIM, int NS, class KRow, class KTap>
 __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, const SortedPts<T>& pts,
                                                const cplx_t<T>* cin, KRow krow, KTap ktap,
-                                               bool prefix_only = false) {
+                                               int nd = 0) {
   using C = cplx_t<T>;
   constexpr int NT = run_taps<DIM, NS>();
   constexpr int KV = DIM * NS;
@@ -1094,14 +1094,15 @@ __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, 
   // (points on the window's first cell) has at least dense_run(DIM) points is
   // accumulated -- the run's first n <= 32 points -- and the cursor moves by
   // n, so the next window starts at a run boundary; any other window is
-  // spread point by point and the cursor moves by 32.  prefix_only: the
-  // points are a subproblem's dense prefix (every cell holds a run), so a
+  // spread point by point and the cursor moves by 32.  Inside the
+  // subproblem's dense prefix (its first nd points, every cell a run) a
   // leading run of at least 4 points is accumulated too, and a shorter one
-  // (a run's remainder) is spread point by point alone: the cursor never
-  // leaves a run boundary.
-  const int kMinRun = prefix_only ? 4 : dense_run(DIM);
+  // (a run's remainder) is spread point by point alone: there the cursor
+  // never leaves a run boundary.
   int cs = beg;
   while (cs < end) {  // warp-uniform
+    const bool in_prefix = cs < nd;
+    const int kMinRun = in_prefix ? 4 : dense_run(DIM);
     const int ql = cs + lane;
     const bool valid = ql < end;
     const int p = st.p0 + (valid ? ql : cs);
@@ -1224,7 +1225,7 @@ __device__ __forceinline__ void run_subproblem(const SubTile& st, T* re, T* im, 
       const int g = lane / L, j = lane % L;
       const bool tap = j < NS;
       const int jj = tap ? j : 0;
-      const int lim = prefix_only ? nrun : 32;  // points of this window
+      const int lim = in_prefix ? nrun : 32;  // points of this window
       // cell-ordered neighbours overlap: group g takes points it + g * NIT,
       // so the PPW points of one warp instruction lie far apart in the chunk
       const int NIT = (lim + PPW - 1) / PPW;
@@ -1268,7 +1269,8 @@ k_spread_sm_run(SpreadArgs<T> a, int split) {
   if (a.sub_dense && !a.sub_dense[blockIdx.x]) return;  // sparse: done by k_spread_sm_wc / slab
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SubTile st = sub_tile_block<DIM, NS>(a.bins, blockIdx.x);
-  if (split) st.np = a.sub_ndense[blockIdx.x];  // the rest: k_spread_sm_slab
+  const int nd = a.sub_ndense ? a.sub_ndense[blockIdx.x] : 0;  // leading dense points
+  if (split) st.np = nd;  // the rest: k_spread_sm_slab
   T* re = reinterpret_cast<T*>(smem_raw);
   T* im = re + st.ntile;
   const int t = blockIdx.y;
@@ -1278,7 +1280,7 @@ k_spread_sm_run(SpreadArgs<T> a, int split) {
   run_subproblem<T, DIM, NS>(
       st, re, im, a.pts, a.c_in + (size_t)t * a.M,
       [&](T dv, T* out) { kernel_row<T, NS, HD>(dv, kc, out); },
-      [&](T dv, int j) { return kernel_tap<T, NS, HD>(dv, j, kc); }, split != 0);
+      [&](T dv, int j) { return kernel_tap<T, NS, HD>(dv, j, kc); }, nd);
   __syncthreads();
   plane_flush<T>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g);
 }

@@ -206,28 +206,8 @@ void orc_fseries(int nf, int ns, double beta, double c, double* fwkerhalf) {
   }
 }
 
-/* RESCALE macro with pirange=1, contrib/spreadinterp.h:36-38: maps
- * x in [-3pi,3pi) to [0,N) folding one period on each side. */
-static inline double orc_rescale(double x, int N) {
-  double sh = (x < -ORC_PI) ? 1.5 : (x >= ORC_PI ? -0.5 : 0.5);
-  return (x * ORC_1_2PI + sh) * (double)N;
-}
-
 static inline int orc_wrap(int i, int n) {
   return i < 0 ? i + n : (i >= n ? i - n : i);
-}
-
-/* Kernel values along one dimension for the taps start..start+ns-1 of a
- * point at rescaled position xr; start = ceil(xr - ns/2).  Restates
- * eval_kernel_vec (src/cuspreadinterp.h:33-40).  The reference loops
- * xstart..xend, which is ns taps unless xr-ns/2 is an integer; the extra tap
- * then has kernel value 0, so ns taps carry the whole sum. */
-static inline int orc_taps(double xr, int ns, double beta, double c,
-                           double* ker) {
-  int start = (int)ceil(xr - ns / 2.0);
-  for (int j = 0; j < ns; ++j)
-    ker[j] = orc_es_kernel((double)(start + j) - xr, ns, beta, c);
-  return start;
 }
 
 /* Coloured bin schedule for a race-free parallel spread: bins of width bs
@@ -246,168 +226,16 @@ static inline int orc_colour(int b, int nb) {
   return b % 2;
 }
 
-/* Type-1 spread (spread_direction 1) of ntr transforms:
- * fw[t][cell] += c[t][j] * prod_d phi(cell_d - xr_d), restating
- * Spread_{1,2,3}d_NUptsdriven (src/2d/spreadinterp2d.cu:16-57,
- * src/3d/spreadinterp3d.cu:73-127, src/1d/spreadinterp1d.cu:16-44).
- * fw must be zeroed by the caller.  x/y/z are FP64 copies of the user's
- * coordinates in [-3pi,3pi). */
-void orc_spread(int dim, int nf1, int nf2, int nf3, int M, const double* x,
-                const double* y, const double* z, int ntr, const double* c,
-                double* fw, int ns, double beta, double es_c) {
-  int nf[3] = {nf1, dim > 1 ? nf2 : 1, dim > 2 ? nf3 : 1};
-  int bs[3], nb[3];
-  int bdef = dim == 1 ? 256 : (dim == 2 ? 32 : 16);
-  for (int d = 0; d < 3; ++d) {
-    bs[d] = d < dim ? (bdef < ns ? ns : bdef) : 1;
-    if (d < dim && bs[d] > nf[d]) bs[d] = nf[d];
-    nb[d] = (nf[d] + bs[d] - 1) / bs[d];
-    if (nb[d] > 1 && nf[d] - (nb[d] - 1) * bs[d] < ns - 1) nb[d] -= 1;
-  }
-  long long nbins = (long long)nb[0] * nb[1] * nb[2];
-  /* bin every point by its first tap */
-  int* bin = (int*)malloc(sizeof(int) * (size_t)(M > 0 ? M : 1));
-  long long* cnt = (long long*)calloc((size_t)nbins + 1, sizeof(long long));
-  for (int j = 0; j < M; ++j) {
-    const double* co[3] = {x, y, z};
-    int bidx[3] = {0, 0, 0};
-    for (int d = 0; d < dim; ++d) {
-      double xr = orc_rescale(co[d][j], nf[d]);
-      int s = (int)ceil(xr - ns / 2.0);
-      s = ((s % nf[d]) + nf[d]) % nf[d];
-      bidx[d] = s / bs[d] < nb[d] ? s / bs[d] : nb[d] - 1;
-    }
-    bin[j] = bidx[0] + nb[0] * (bidx[1] + nb[1] * bidx[2]);
-    cnt[bin[j] + 1]++;
-  }
-  for (long long b = 0; b < nbins; ++b) cnt[b + 1] += cnt[b];
-  int* order = (int*)malloc(sizeof(int) * (size_t)(M > 0 ? M : 1));
-  long long* fill = (long long*)malloc(sizeof(long long) * (size_t)nbins);
-  memcpy(fill, cnt, sizeof(long long) * (size_t)nbins);
-  for (int j = 0; j < M; ++j) order[fill[bin[j]]++] = j;
-  free(fill);
-  size_t Nf = (size_t)nf[0] * nf[1] * nf[2];
-  for (int colour = 0; colour < 27; ++colour) {
-    int cz = colour / 9, cy = (colour / 3) % 3, cx = colour % 3;
-    if ((dim < 3 && cz) || (dim < 2 && cy)) continue;
-#pragma omp parallel for schedule(dynamic, 1)
-    for (long long b = 0; b < nbins; ++b) {
-      int bx = (int)(b % nb[0]), by = (int)((b / nb[0]) % nb[1]),
-          bz = (int)(b / ((long long)nb[0] * nb[1]));
-      if (orc_colour(bx, nb[0]) != cx || orc_colour(by, nb[1]) != cy ||
-          orc_colour(bz, nb[2]) != cz)
-        continue;
-      double k1[ORC_MAX_NSPREAD], k2[ORC_MAX_NSPREAD], k3[ORC_MAX_NSPREAD];
-      for (long long p = cnt[b]; p < cnt[b + 1]; ++p) {
-        int j = order[p];
-        int s1 = orc_taps(orc_rescale(x[j], nf[0]), ns, beta, es_c, k1);
-        int s2 = 0, s3 = 0;
-        int n2 = 1, n3 = 1;
-        k2[0] = 1.0;
-        k3[0] = 1.0;
-        if (dim > 1) { s2 = orc_taps(orc_rescale(y[j], nf[1]), ns, beta, es_c, k2); n2 = ns; }
-        if (dim > 2) { s3 = orc_taps(orc_rescale(z[j], nf[2]), ns, beta, es_c, k3); n3 = ns; }
-        for (int t = 0; t < ntr; ++t) {
-          double cr = c[2 * ((size_t)t * M + j)], ci = c[2 * ((size_t)t * M + j) + 1];
-          double* g = fw + 2 * Nf * (size_t)t;
-          for (int dz = 0; dz < n3; ++dz) {
-            int iz = dim > 2 ? orc_wrap(s3 + dz, nf[2]) : 0;
-            for (int dy = 0; dy < n2; ++dy) {
-              int iy = dim > 1 ? orc_wrap(s2 + dy, nf[1]) : 0;
-              double kyz = k2[dy] * k3[dz];
-              size_t row = ((size_t)iz * nf[1] + iy) * nf[0];
-              for (int dx = 0; dx < ns; ++dx) {
-                int ix = orc_wrap(s1 + dx, nf[0]);
-                double kv = k1[dx] * kyz;
-                g[2 * (row + ix)] += cr * kv;
-                g[2 * (row + ix) + 1] += ci * kv;
-              }
-            }
-          }
-        }
-      }
-    }
-  }
-  free(order);
-  free(cnt);
-  free(bin);
-}
-
-/* Type-2 interpolation: c[t][j] = sum_cells fw[t][cell] * prod_d
- * phi(cell_d - xr_d), restating Interp_{1,2,3}d_NUptsdriven
- * (src/2d/spreadinterp2d.cu:516-553, src/3d/spreadinterp3d.cu:654-703,
- * src/1d/spreadinterp1d.cu:233-258). */
-void orc_interp(int dim, int nf1, int nf2, int nf3, int M, const double* x,
-                const double* y, const double* z, int ntr, double* c,
-                const double* fw, int ns, double beta, double es_c) {
-  int nf[3] = {nf1, dim > 1 ? nf2 : 1, dim > 2 ? nf3 : 1};
-  size_t Nf = (size_t)nf[0] * nf[1] * nf[2];
-#pragma omp parallel for schedule(static)
-  for (int j = 0; j < M; ++j) {
-    double k1[ORC_MAX_NSPREAD], k2[ORC_MAX_NSPREAD], k3[ORC_MAX_NSPREAD];
-    int s1 = orc_taps(orc_rescale(x[j], nf[0]), ns, beta, es_c, k1);
-    int s2 = 0, s3 = 0, n2 = 1, n3 = 1;
-    k2[0] = 1.0;
-    k3[0] = 1.0;
-    if (dim > 1) { s2 = orc_taps(orc_rescale(y[j], nf[1]), ns, beta, es_c, k2); n2 = ns; }
-    if (dim > 2) { s3 = orc_taps(orc_rescale(z[j], nf[2]), ns, beta, es_c, k3); n3 = ns; }
-    for (int t = 0; t < ntr; ++t) {
-      const double* g = fw + 2 * Nf * (size_t)t;
-      double ar = 0.0, ai = 0.0;
-      for (int dz = 0; dz < n3; ++dz) {
-        int iz = dim > 2 ? orc_wrap(s3 + dz, nf[2]) : 0;
-        for (int dy = 0; dy < n2; ++dy) {
-          int iy = dim > 1 ? orc_wrap(s2 + dy, nf[1]) : 0;
-          double kyz = k2[dy] * k3[dz];
-          size_t row = ((size_t)iz * nf[1] + iy) * nf[0];
-          for (int dx = 0; dx < ns; ++dx) {
-            int ix = orc_wrap(s1 + dx, nf[0]);
-            double kv = k1[dx] * kyz;
-            ar += g[2 * (row + ix)] * kv;
-            ai += g[2 * (row + ix) + 1] * kv;
-          }
-        }
-      }
-      c[2 * ((size_t)t * M + j)] = ar;
-      c[2 * ((size_t)t * M + j) + 1] = ai;
-    }
-  }
-}
-
-/* Deconvolution (type 1) and amplification (type 2), restating
- * Deconvolve_{1,2,3}d / Amplify_{1,2,3}d (src/deconvolve_wrapper.cu:14-121):
- * mode k_d (index i_d in 0..N_d-1, k_d = i_d - N_d/2) sits at fine-grid
- * index k_d mod nf_d and is divided by prod_d fwkerhalf_d[|k_d|].
- * dir 1: fk = fw / ker.  dir 2: fw = 0 everywhere, then fw[mode] = fk / ker. */
-void orc_deconvolve(int dir, int dim, int ms, int mt, int mu, int nf1, int nf2,
-                    int nf3, int ntr, double* fw, double* fk,
-                    const double* ker1, const double* ker2,
-                    const double* ker3) {
-  int N[3] = {ms, dim > 1 ? mt : 1, dim > 2 ? mu : 1};
-  int nf[3] = {nf1, dim > 1 ? nf2 : 1, dim > 2 ? nf3 : 1};
-  size_t Nf = (size_t)nf[0] * nf[1] * nf[2];
-  size_t Nm = (size_t)N[0] * N[1] * N[2];
-  if (dir == 2) memset(fw, 0, sizeof(double) * 2 * Nf * (size_t)ntr);
-#pragma omp parallel for schedule(static)
-  for (long long m = 0; m < (long long)Nm; ++m) {
-    int i1 = (int)(m % N[0]), i2 = (int)((m / N[0]) % N[1]),
-        i3 = (int)(m / ((long long)N[0] * N[1]));
-    int k1 = i1 - N[0] / 2, k2 = i2 - N[1] / 2, k3 = i3 - N[2] / 2;
-    int w1 = k1 >= 0 ? k1 : nf[0] + k1;
-    int w2 = k2 >= 0 ? k2 : nf[1] + k2;
-    int w3 = k3 >= 0 ? k3 : nf[2] + k3;
-    double kv = ker1[abs(k1)];
-    if (dim > 1) kv *= ker2[abs(k2)];
-    if (dim > 2) kv *= ker3[abs(k3)];
-    size_t widx = ((size_t)w3 * nf[1] + w2) * nf[0] + w1;
-    for (int t = 0; t < ntr; ++t) {
-      double* g = fw + 2 * (Nf * (size_t)t + widx);
-      double* f = fk + 2 * (Nm * (size_t)t + (size_t)m);
-      if (dir == 1) { f[0] = g[0] / kv; f[1] = g[1] / kv; }
-      else { g[0] = f[0] / kv; g[1] = f[1] / kv; }
-    }
-  }
-}
+#define ORC_R double
+#define ORC_SFX(n) n
+#include "oracle_stages.inc"
+#undef ORC_R
+#undef ORC_SFX
+#define ORC_R float
+#define ORC_SFX(n) n##_f32
+#include "oracle_stages.inc"
+#undef ORC_R
+#undef ORC_SFX
 
 /* FP64 direct sums (the accuracy oracle), restating contrib/dirft2d.cpp:7-64
  * (dirft2d1/dirft2d2) for any dimension, with each phase computed directly

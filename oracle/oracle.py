@@ -31,6 +31,7 @@ _LIB = None
 _LOCK = threading.Lock()
 
 _d_p = ctypes.POINTER(ctypes.c_double)
+_f_p = ctypes.POINTER(ctypes.c_float)
 _ll_p = ctypes.POINTER(ctypes.c_longlong)
 _i_p = ctypes.POINTER(ctypes.c_int)
 
@@ -73,6 +74,12 @@ def lib() -> ctypes.CDLL:
                                                                              _ll_p, _d_p]
             L.orc_dirft_type3.argtypes = [ctypes.c_int, ctypes.c_int] + [_d_p] * 7 + [
                 ctypes.c_int, ctypes.c_int, _ll_p, _d_p]
+            # FP32-arithmetic stages (the CPU timing of FP32 workloads)
+            L.orc_spread_f32.argtypes = [ctypes.c_int] * 5 + [_f_p] * 3 + [ctypes.c_int, _f_p, _f_p,
+                                                                          ctypes.c_int, ctypes.c_double,
+                                                                          ctypes.c_double]
+            L.orc_interp_f32.argtypes = L.orc_spread_f32.argtypes
+            L.orc_deconvolve_f32.argtypes = [ctypes.c_int] * 9 + [_f_p, _f_p, _d_p, _d_p, _d_p]
             L.orc_num_threads.restype = ctypes.c_int
             L.orc_set_num_threads.argtypes = [ctypes.c_int]
             _LIB = L
@@ -81,6 +88,10 @@ def lib() -> ctypes.CDLL:
 
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(_d_p)
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(_f_p)
 
 
 def _f64(a) -> np.ndarray:
@@ -155,7 +166,11 @@ class OraclePlan:
 
     def __init__(self, nufft_type: int, modes, iflag: int, tol: float, single: bool,
                  gpu_method: int = 0, obin: tuple = (8, 8, 8), spreadinterponly: bool = False,
-                 upsampfac: float = 2.0, ns: int | None = None):
+                 upsampfac: float = 2.0, ns: int | None = None, fp32_arith: bool = False):
+        # fp32_arith: spread, interpolation, FFT and deconvolution in FP32
+        # (the CPU form of the reference's FP32 build, for timing FP32
+        # workloads); the default is FP64 arithmetic, the accuracy oracle
+        self.fp32 = bool(fp32_arith)
         self.type = int(nufft_type)
         self.modes = tuple(int(m) for m in modes)
         self.dim = len(self.modes)
@@ -181,12 +196,17 @@ class OraclePlan:
         self.ker = [fseries(nf, self.ns, self.beta, self.c) for nf in self.nf]
 
     def _pts(self, x, y, z):
-        pts = [_f64(x)]
+        rd = np.float32 if self.fp32 else np.float64
+        cv = (lambda a: np.ascontiguousarray(np.asarray(a, dtype=rd)))
+        pts = [cv(x)]
         M = pts[0].size
-        dummy = np.zeros(max(M, 1))
-        pts.append(_f64(y) if self.dim > 1 else dummy)
-        pts.append(_f64(z) if self.dim > 2 else dummy)
+        dummy = np.zeros(max(M, 1), dtype=rd)
+        pts.append(cv(y) if self.dim > 1 else dummy)
+        pts.append(cv(z) if self.dim > 2 else dummy)
         return M, pts
+
+    def _cplx(self, a) -> np.ndarray:
+        return np.ascontiguousarray(np.asarray(a, dtype=np.complex64 if self.fp32 else np.complex128))
 
     def _nf3(self):
         nf = list(self.nf) + [1] * (3 - self.dim)
@@ -210,49 +230,56 @@ class OraclePlan:
             return np.fft.ifftn(fw, axes=axes, norm="forward")
         return np.fft.fftn(fw, axes=axes)
 
+    def _stage(self, name):
+        # (C function, real view, pointer cast) of the plan's arithmetic
+        if self.fp32:
+            return getattr(lib(), name + "_f32"), np.float32, _fp
+        return getattr(lib(), name), np.float64, _dp
+
     def spread(self, x, y, z, c, ntr: int = 1) -> np.ndarray:
         M, (px, py, pz) = self._pts(x, y, z)
         nf = self._nf3()
-        cc = _c128(c).reshape(ntr, M)
-        fw = np.zeros((ntr, nf[2], nf[1], nf[0]), dtype=np.complex128)
-        lib().orc_spread(self.dim, nf[0], nf[1], nf[2], M, _dp(px), _dp(py), _dp(pz), ntr,
-                         _dp(cc.view(np.float64)), _dp(fw.view(np.float64)), self.ns, self.beta,
-                         self.c)
+        cc = self._cplx(c).reshape(ntr, M)
+        fw = np.zeros((ntr, nf[2], nf[1], nf[0]), dtype=cc.dtype)
+        fn, rv, pp = self._stage("orc_spread")
+        fn(self.dim, nf[0], nf[1], nf[2], M, pp(px), pp(py), pp(pz), ntr, pp(cc.view(rv)),
+           pp(fw.view(rv)), self.ns, self.beta, self.c)
         return fw
 
     def interp(self, x, y, z, fw: np.ndarray, ntr: int = 1) -> np.ndarray:
         M, (px, py, pz) = self._pts(x, y, z)
         nf = self._nf3()
-        g = _c128(fw).reshape(ntr, nf[2], nf[1], nf[0])
-        c = np.zeros((ntr, M), dtype=np.complex128)
-        lib().orc_interp(self.dim, nf[0], nf[1], nf[2], M, _dp(px), _dp(py), _dp(pz), ntr,
-                         _dp(c.view(np.float64)), _dp(g.view(np.float64)), self.ns, self.beta,
-                         self.c)
+        g = self._cplx(fw).reshape(ntr, nf[2], nf[1], nf[0])
+        c = np.zeros((ntr, M), dtype=g.dtype)
+        fn, rv, pp = self._stage("orc_interp")
+        fn(self.dim, nf[0], nf[1], nf[2], M, pp(px), pp(py), pp(pz), ntr, pp(c.view(rv)),
+           pp(g.view(rv)), self.ns, self.beta, self.c)
         return c
 
     def _deconv(self, direction: int, fw: np.ndarray, fk: np.ndarray, ntr: int):
         nf = self._nf3()
         N = self._modes3()
         kers = [self.ker[d] if d < self.dim else np.ones(1) for d in range(3)]
-        lib().orc_deconvolve(direction, self.dim, N[0], N[1], N[2], nf[0], nf[1], nf[2], ntr,
-                             _dp(fw.view(np.float64)), _dp(fk.view(np.float64)), _dp(kers[0]),
-                             _dp(kers[1]), _dp(kers[2]))
+        fn, rv, pp = self._stage("orc_deconvolve")
+        fn(direction, self.dim, N[0], N[1], N[2], nf[0], nf[1], nf[2], ntr, pp(fw.view(rv)),
+           pp(fk.view(rv)), _dp(kers[0]), _dp(kers[1]), _dp(kers[2]))
 
     def execute(self, x, y=None, z=None, data=None, ntr: int = 1) -> np.ndarray:
         """Type 1: data = c (ntr*M) -> fk (ntr, N3, N2, N1).  Type 2: data = fk
         (ntr*N) -> c (ntr, M)."""
         N = self._modes3()
+        cdt = np.complex64 if self.fp32 else np.complex128
         if self.type == 1:
             fw = self.spread(x, y, z, data, ntr)
-            fw = np.ascontiguousarray(self._fft(fw))
-            fk = np.zeros((ntr, N[2], N[1], N[0]), dtype=np.complex128)
+            fw = np.ascontiguousarray(self._fft(fw), dtype=cdt)
+            fk = np.zeros((ntr, N[2], N[1], N[0]), dtype=cdt)
             self._deconv(1, fw, fk, ntr)
             return fk
         nf = self._nf3()
-        fk = _c128(data).reshape(ntr, N[2], N[1], N[0]).copy()
-        fw = np.zeros((ntr, nf[2], nf[1], nf[0]), dtype=np.complex128)
+        fk = self._cplx(data).reshape(ntr, N[2], N[1], N[0]).copy()
+        fw = np.zeros((ntr, nf[2], nf[1], nf[0]), dtype=cdt)
         self._deconv(2, fw, fk, ntr)
-        fw = np.ascontiguousarray(self._fft(fw))
+        fw = np.ascontiguousarray(self._fft(fw), dtype=cdt)
         return self.interp(x, y, z, fw, ntr)
 
 

@@ -207,3 +207,22 @@ def test_oracle_spread_independent_of_threads(modes, ns):
     finally:
         O.set_num_threads(nthr)
     assert np.array_equal(serial, parallel)
+
+
+@pytest.mark.parametrize("ntype,modes", [(1, (40,)), (2, (24, 20)), (1, (12, 10, 8))])
+def test_fp32_arith_form_matches_fp64(ntype, modes):
+    """The FP32-arithmetic form of the oracle (the CPU timing of FP32
+    workloads) computes the same transform: within FP32 rounding of the
+    rescaled coordinates (a few 1e-6 at these sizes) of the FP64 oracle."""
+    rng = np.random.default_rng(40 + ntype)
+    dim, M = len(modes), 3000
+    pts = [rng.uniform(-3 * np.pi, 3 * np.pi, M) for _ in range(dim)] + [None] * (3 - dim)
+    data = (rng.standard_normal(M) + 1j * rng.standard_normal(M) if ntype == 1 else
+            rng.standard_normal(int(np.prod(modes))) + 1j * rng.standard_normal(int(np.prod(modes))))
+    iflag = 1 if ntype == 1 else -1
+    p64 = O.OraclePlan(ntype, modes, iflag, 1e-6, True)
+    p32 = O.OraclePlan(ntype, modes, iflag, 1e-6, True, fp32_arith=True)
+    a = p64.execute(*pts, data=data)
+    b = p32.execute(*pts, data=data)
+    assert b.dtype == np.complex64 and a.dtype == np.complex128
+    assert np.linalg.norm(b - a) / np.linalg.norm(a) < 5e-5
