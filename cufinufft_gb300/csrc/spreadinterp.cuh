@@ -1039,6 +1039,156 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
   plane_flush<T>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g, PX);
 }
 
+// ---------------------------------------------------------------------------
+// Private-tile 2D spreading (method 2, the default for 2D subproblems).  A 2D
+// tile is small (39 x 40 cells at ns 8 with 32 x 32 bins), so each of the
+// block's kPrivWarps warps accumulates its share of the subproblem's points
+// into a private copy with plain shared loads and stores -- lanes over the
+// point's (x, y) taps, 32 / NS rows per instruction, a __syncwarp between
+// points -- and the copies are summed cell by cell once at the end (one
+// thread per cell, no atomics) and flushed.  Each warp stages the kernel rows
+// of 32 points at a time in warp-private shared memory (c kx as complex, ky,
+// the tile offset): lane q evaluates point q's rows.  Rows are padded to a
+// pitch of +-NS (mod 32), so the rows of one instruction fall in disjoint
+// banks.  Results equal the atomic kernel's up to the order of additions.
+constexpr int kPrivWarps = 4;
+
+__host__ __device__ constexpr int priv_pitch(int tx, int ns) {
+  // smallest pitch >= tx that is ns or 32 - ns (mod 32)
+  return ((tx % 32) <= ns) ? tx + (ns - tx % 32) : ((tx % 32) <= 32 - ns ? tx + (32 - ns - tx % 32)
+                                                                         : tx + (32 - tx % 32) + ns);
+}
+
+template <typename T>
+size_t priv_bytes(int ns, const BinTables& bt) {
+  const size_t px = priv_pitch(bt.bs[0] + ns - 1, ns);
+  const size_t copy = px * (bt.bs[1] + ns - 1) * 2 * sizeof(T);          // re and im planes
+  const size_t stage = 32 * (size_t)ns * (sizeof(cplx_t<T>) + sizeof(T)) + 32 * sizeof(int);
+  return kPrivWarps * (((copy + 15) & ~(size_t)15) + ((stage + 15) & ~(size_t)15));
+}
+
+template <typename T, int NS>
+__global__ void __launch_bounds__(32 * kPrivWarps)
+k_spread_sm_priv(SpreadArgs<T> a, int split) {
+  using C = cplx_t<T>;
+  constexpr int R = 32 / NS;                 // tile rows per warp instruction
+  constexpr int NR = (NS + R - 1) / R;       // instructions per point
+  constexpr int HD = horner_degree<T>(NS);
+  int first = 0;
+  if (a.sub_dense && a.sub_dense[blockIdx.x]) {  // cell-run layout: dense prefixes by k_spread_sm_run
+    if (!split) return;
+    first = a.sub_ndense[blockIdx.x];
+  }
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const SubTile st = sub_tile_block<2, NS>(a.bins, blockIdx.x);
+  if (first >= st.np) return;  // block-uniform
+  const int PX = priv_pitch(st.TX, NS);
+  const int ncell = PX * st.TY;
+  const size_t copy_sz = ((size_t)ncell * 2 * sizeof(T) + 15) & ~(size_t)15;
+  const size_t stage_sz = ((size_t)32 * NS * (sizeof(C) + sizeof(T)) + 32 * sizeof(int) + 15) & ~(size_t)15;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* re = reinterpret_cast<T*>(smem_raw + warp * copy_sz);
+  T* im = re + ncell;
+  unsigned char* sb = smem_raw + kPrivWarps * copy_sz + warp * stage_sz;
+  C* s_ck = reinterpret_cast<C*>(sb);
+  T* s_ky = reinterpret_cast<T*>(s_ck + 32 * NS);
+  int* s_base = reinterpret_cast<int*>(s_ky + 32 * NS);
+  for (int i = lane; i < 2 * ncell; i += 32) re[i] = T(0);
+  const int t = blockIdx.y;
+  const C* cin = a.c_in + (size_t)t * a.M;
+  const int dx = lane % NS, dyl = lane / NS;
+  const bool lane_on = lane < R * NS;
+  // warp w takes points first + [w S, (w + 1) S) of the subproblem
+  const int npts = st.np - first;
+  const int S = (npts + kPrivWarps - 1) / kPrivWarps;
+  const int beg = first + warp * S, end = min(st.np, beg + S);
+  // lane q holds point q of the next chunk in registers (loaded while the
+  // current chunk's points are added), then stages its kernel rows
+  T d0 = T(0), d1 = T(0);
+  int i00 = 0, i01 = 0;
+  C cv = C{T(0), T(0)};
+  auto load_pt = [&](int c0) {
+    if (c0 + lane < end) {
+      const int p = st.p0 + c0 + lane;
+      d0 = a.pts.d[0][p];
+      d1 = a.pts.d[1][p];
+      i00 = a.pts.i0[0][p];
+      i01 = a.pts.i0[1][p];
+      cv = cin[a.pts.idx[p]];
+    }
+  };
+  if (beg < end) load_pt(beg);
+  for (int c0 = beg; c0 < end; c0 += 32) {
+    const int nq = min(32, end - c0);
+    __syncwarp();  // the previous chunk's reads of the stage are done
+    if (lane < nq) {
+      T kr[NS];
+      kernel_row<T, NS, HD>(d0, a.kc, kr);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) s_ck[lane * NS + j] = C{cv.x * kr[j], cv.y * kr[j]};
+      kernel_row<T, NS, HD>(d1, a.kc, kr);
+#pragma unroll
+      for (int j = 0; j < NS; ++j) s_ky[lane * NS + j] = kr[j];
+      s_base[lane] = (i01 - st.oy) * PX + (i00 - st.ox);
+    }
+    if (c0 + 32 < end) load_pt(c0 + 32);
+    __syncwarp();
+    // the next point's staged values are read while this point's cells are
+    // read, added to and written
+    C ck = s_ck[dx];
+    int base = s_base[0] + dx;
+    T ky[NR];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) ky[r] = s_ky[min(r * R + dyl, NS - 1)];
+    for (int q = 0; q < nq; ++q) {
+      const int qn = min(q + 1, nq - 1);
+      const C ckn = s_ck[qn * NS + dx];
+      const int basen = s_base[qn] + dx;
+      T kyn[NR];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) kyn[r] = s_ky[qn * NS + min(r * R + dyl, NS - 1)];
+#pragma unroll
+      for (int r = 0; r < NR; ++r) {
+        const int dy = r * R + dyl;
+        if (lane_on && dy < NS) {
+          const int o = base + dy * PX;
+          re[o] = fma_rn(ck.x, ky[r], re[o]);
+          im[o] = fma_rn(ck.y, ky[r], im[o]);
+        }
+      }
+      __syncwarp();  // this point's stores before the next point's loads
+      ck = ckn;
+      base = basen;
+#pragma unroll
+      for (int r = 0; r < NR; ++r) ky[r] = kyn[r];
+    }
+  }
+  __syncthreads();
+  // sum the private copies into copy 0, one thread per cell
+  T* re0 = reinterpret_cast<T*>(smem_raw);
+  T* im0 = re0 + ncell;
+  for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
+    T sr = re0[i], si = im0[i];
+#pragma unroll
+    for (int w = 1; w < kPrivWarps; ++w) {
+      const T* rw = reinterpret_cast<const T*>(smem_raw + w * copy_sz);
+      sr += rw[i];
+      si += rw[i + ncell];
+    }
+    re0[i] = sr;
+    im0[i] = si;
+  }
+  __syncthreads();
+  plane_flush<T>(re0, im0, a.fw + (size_t)t * a.g.Nf, st, a.g, PX);
+}
+
+// CUFINUFFT_SPREAD_PRIV=0: 2D subproblem spreading by the warp-cooperative
+// atomic kernel instead of the private-tile one.
+inline bool priv_spread_enabled() {
+  const char* v = std::getenv("CUFINUFFT_SPREAD_PRIV");
+  return !(v && v[0] == '0');
+}
+
 // CUFINUFFT_SPREAD_SLAB=0: 3D subproblem spreading by the warp-cooperative
 // atomic kernel instead of the slab-owned one.
 inline bool slab_spread_enabled() {
@@ -1611,7 +1761,18 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
   } else {
     if (a.bins.nsub == 0) return cudaSuccess;
     // 3D sparse subproblems: the slab-owned kernel unless a variant is forced
-    bool slab = false, split = false;
+    bool slab = false, split = false, priv = false;
+    if constexpr (DIM == 2) {
+      priv = a.variant == 0 && priv_spread_enabled();
+      if (priv) {  // the private copies and stages must fit (else the atomic kernel)
+        int dev = 0, optin = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e != cudaSuccess) return e;
+        priv = priv_bytes<T>(NS, a.bins) <= (size_t)optin;
+      }
+      split = priv && a.run && a.sub_ndense != nullptr;
+    }
     if constexpr (DIM == 3) {
       slab = a.variant == 0 && slab_spread_enabled();
       if (slab) {  // its padded tile and staging must fit (else the atomic kernel)
@@ -1628,6 +1789,15 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
       split = slab && a.run && a.sub_ndense != nullptr && !tc;
     }
     auto sparse = [&]() -> cudaError_t {
+      if constexpr (DIM == 2) {
+        if (priv) {
+          const size_t smb = priv_bytes<T>(NS, a.bins);
+          cudaError_t e = prepare_smem(k_spread_sm_priv<T, NS>, smb);
+          if (e != cudaSuccess) return e;
+          k_spread_sm_priv<T, NS><<<dim3(a.bins.nsub, a.ntr), 32 * kPrivWarps, smb, s>>>(a, split ? 1 : 0);
+          return cudaGetLastError();
+        }
+      }
       if constexpr (DIM == 3) {
         if (slab) {
           const size_t smb = slab_bytes<T>(NS, a.bins);
@@ -1666,7 +1836,7 @@ cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
       }
     }
     if (a.run) return cudaErrorInvalidValue;  // more than 512 taps per point
-    if (slab) return sparse();
+    if (slab || priv) return sparse();
     size_t sm = tile_bytes<T, DIM>(NS, a.bins);
     cudaError_t e = wc ? prepare_smem(k_spread_sm_wc<T, DIM, NS>, sm)
                        : prepare_smem(k_spread_sm<T, DIM, NS>, sm);
