@@ -993,6 +993,7 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int dx = lane % NS, dyl = lane / NS;
   const bool lane_on = lane < R * NS;
+  constexpr bool kFullRows = 32 % NS == 0 && (NS * NS) % 32 == 0;  // ns 8, 16: all lanes, rows in range
   for (int c0 = first, buf = 0; c0 < st.np; c0 += CH, buf ^= 1) {
     unsigned char* sb = stage0 + buf * stage_sz;
     C* s_ck = reinterpret_cast<C*>(sb);
@@ -1025,7 +1026,7 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
         const int dy = r * R + dyl;
-        if (lane_on && dy < NS) {
+        if (kFullRows || (lane_on && dy < NS)) {
           const T ky = s_ky[q * NS + dy];
           const int o = base + dy * PX;
           re[o] = fma_rn(ur, ky, re[o]);
@@ -1098,6 +1099,7 @@ k_spread_sm_priv(SpreadArgs<T> a, int split) {
   const C* cin = a.c_in + (size_t)t * a.M;
   const int dx = lane % NS, dyl = lane / NS;
   const bool lane_on = lane < R * NS;
+  constexpr bool kFullRows = 32 % NS == 0 && (NS * NS) % 32 == 0;  // ns 8, 16: all lanes, rows in range
   // warp w takes points first + [w S, (w + 1) S) of the subproblem
   const int npts = st.np - first;
   const int S = (npts + kPrivWarps - 1) / kPrivWarps;
@@ -1150,7 +1152,7 @@ k_spread_sm_priv(SpreadArgs<T> a, int split) {
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
         const int dy = r * R + dyl;
-        if (lane_on && dy < NS) {
+        if (kFullRows || (lane_on && dy < NS)) {
           const int o = base + dy * PX;
           re[o] = fma_rn(ck.x, ky[r], re[o]);
           im[o] = fma_rn(ck.y, ky[r], im[o]);

@@ -22,6 +22,7 @@ def _rel(a, b):
 CASES = [
     # modes, M, single, tol, bins, ntr
     ((64, 60), 30000, True, 1e-6, (32, 32), 1),
+    ((64, 60), 30000, True, 1e-6, (16, 16), 2, "tol"),   # ns 8: full-lane rows
     ((64, 60), 30000, True, 1e-2, (16, 16), 3),
     ((90, 70), 40000, True, 1e-4, (64, 64), 2),
     ((50, 70), 20000, True, 1e-5, (24, 40), 1),
@@ -31,20 +32,24 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("modes,M,single,tol,bins,ntr", CASES)
-def test_priv_spread(monkeypatch, modes, M, single, tol, bins, ntr):
+@pytest.mark.parametrize("case", CASES)
+def test_priv_spread(monkeypatch, case):
+    modes, M, single, tol, bins, ntr = case[:6]
+    rule = case[6] if len(case) > 6 else None
     rng = np.random.default_rng(int(1e6 * tol) % 89 + M)
     dt = np.float32 if single else np.float64
     pts = NC.points(rng, 2, M, lo=-3 * np.pi, hi=3 * np.pi, dtype=dt, edges=False)
     c = NC.strengths(rng, M, ntr)
     kw = dict(ntr=ntr, gpu_method=2, gpu_binsizex=bins[0], gpu_binsizey=bins[1], maxbatchsize=2)
+    if rule:
+        kw["width_rule"] = rule
     monkeypatch.setenv("CUFINUFFT_SPREAD_PRIV", "0")
     ref_wc, _ = NC.run_gpu(1, modes, pts, c, tol, single, **kw)
     monkeypatch.delenv("CUFINUFFT_SPREAD_PRIV")
     out, info = NC.run_gpu(1, modes, pts, c, tol, single, **kw)
     assert _rel(out, ref_wc) < (1e-6 if single else 1e-13), info
     ref = NC.oracle_nufft(1, modes, [p.astype(np.float64) for p in pts], c, tol, single, ntr=ntr,
-                          gpu_method=2)
+                          gpu_method=2, ns=info["ns"])
     assert _rel(out, ref) < (2e-5 if single else 1e-10), info
 
 

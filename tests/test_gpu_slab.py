@@ -21,6 +21,7 @@ def _rel(a, b):
 CASES = [
     # modes, M, single, tol, method, bins, ntr
     ((24, 20, 18), 20000, True, 1e-6, 2, (16, 16, 2), 1),
+    ((24, 20, 18), 20000, True, 1e-6, 2, (8, 8, 8), 2, "tol"),   # ns 8: full-lane rows
     ((24, 20, 18), 20000, True, 1e-2, 2, (8, 8, 8), 3),
     ((30, 28, 26), 30000, True, 1e-4, 2, (16, 16, 4), 2),
     ((16, 18, 20), 8000, False, 1e-12, 2, (8, 8, 8), 2),
@@ -29,21 +30,25 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize("modes,M,single,tol,method,bins,ntr", CASES)
-def test_slab_spread(monkeypatch, modes, M, single, tol, method, bins, ntr):
+@pytest.mark.parametrize("case", CASES)
+def test_slab_spread(monkeypatch, case):
+    modes, M, single, tol, method, bins, ntr = case[:7]
+    rule = case[7] if len(case) > 7 else None
     rng = np.random.default_rng(int(1e6 * tol) % 97 + M)
     dt = np.float32 if single else np.float64
     pts = NC.points(rng, 3, M, lo=-3 * np.pi, hi=3 * np.pi, dtype=dt, edges=False)
     c = NC.strengths(rng, M, ntr)
     kw = dict(ntr=ntr, gpu_method=method, gpu_binsizex=bins[0], gpu_binsizey=bins[1],
               gpu_binsizez=bins[2], maxbatchsize=2)
+    if rule:
+        kw["width_rule"] = rule
     monkeypatch.setenv("CUFINUFFT_SPREAD_SLAB", "0")
     ref_wc, _ = NC.run_gpu(1, modes, pts, c, tol, single, **kw)
     monkeypatch.delenv("CUFINUFFT_SPREAD_SLAB")
     out, info = NC.run_gpu(1, modes, pts, c, tol, single, **kw)
     assert _rel(out, ref_wc) < (1e-6 if single else 1e-13), info
     ref = NC.oracle_nufft(1, modes, [p.astype(np.float64) for p in pts], c, tol, single, ntr=ntr,
-                          gpu_method=2)
+                          gpu_method=2, ns=info["ns"])
     assert _rel(out, ref) < (2e-5 if single else 1e-10), info
 
 
