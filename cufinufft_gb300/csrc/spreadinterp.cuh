@@ -35,12 +35,18 @@ namespace cfg {
 
 constexpr int kSpreadThreads = 256;
 // Threads of a k_interp_sm block, and the blocks per SM its register bound
-// is set for: FP32 6 (40 registers a thread for ns <= 9; 4 above), FP64 2
-// (128 registers: radial 2D FP64 at ns 13 interpolates 4% faster than at one
-// block of 188 registers, despite 52 bytes of spill).
+// is set for.  FP32: 256 threads, 6 blocks (40 registers a thread for
+// ns <= 9; 4 blocks above).  FP64 plans' subproblem interpolation (FP64 or
+// double-float): 512 threads, one block, the same 128 registers a thread as
+// two 256-thread blocks (which ran radial 2D FP64 at ns 13 4% faster than one
+// block of 188 registers, despite 52 bytes of spill); measured at ns 14, the
+// double-float kernel 1.11 -> 1.01 ms with 512-thread blocks, while FP32 plans
+// keep 256 (34.2 vs 35.1 us at ns 8).
 constexpr int kInterpThreads = 256;
 constexpr int kInterpBlocksF32 = 6 * 256 / kInterpThreads;
-constexpr int kInterpBlocksF64 = 2 * 256 / kInterpThreads;
+constexpr int kInterpThreadsF64 = 512;
+constexpr int kInterpBlocksF64 = 1;
+template <typename T> constexpr int interp_threads() { return sizeof(T) == 4 ? kInterpThreads : kInterpThreadsF64; }
 
 // Subproblem header shared by the shared-memory kernels.
 struct SubTile {
@@ -547,7 +553,7 @@ struct InterpPoint {
 // wait: evaluated before it, the rows stay live across the wait and the FP32
 // kernels spill at the 40-register bound (measured 3.5% slower).
 template <typename T, int DIM, int NS>
-__global__ void __launch_bounds__(kInterpThreads, sizeof(T) == 4 ? (NS <= 9 ? kInterpBlocksF32 : kInterpBlocksF32 * 2 / 3) : kInterpBlocksF64)
+__global__ void __launch_bounds__(interp_threads<T>(), sizeof(T) == 4 ? (NS <= 9 ? kInterpBlocksF32 : kInterpBlocksF32 * 2 / 3) : kInterpBlocksF64)
 k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) {
   using C = cplx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -636,7 +642,7 @@ __device__ __forceinline__ DF df_kernel_tap(double d, int j, const KernelCoeffs<
 }
 
 template <int DIM, int NS>
-__global__ void __launch_bounds__(kInterpThreads, kInterpBlocksF64)
+__global__ void __launch_bounds__(kInterpThreadsF64, kInterpBlocksF64)
 k_interp_sm_df(SpreadArgs<double> a, const __grid_constant__ CUtensorMap gmap, int tma) {
   using C = double2;
   constexpr int HD = horner_degree<double>(NS);
@@ -1887,7 +1893,7 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
       if (!wc && a.fp64_df) {
         cudaError_t e = prepare_smem(k_interp_sm_df<DIM, NS>, sm);
         if (e != cudaSuccess) return e;
-        k_interp_sm_df<DIM, NS><<<dim3(a.bins.nsub, a.ntr), kInterpThreads, sm, s>>>(a, gmap, tma);
+        k_interp_sm_df<DIM, NS><<<dim3(a.bins.nsub, a.ntr), kInterpThreadsF64, sm, s>>>(a, gmap, tma);
         return cudaGetLastError();
       }
     }
@@ -1896,7 +1902,7 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     dim3 grid(a.bins.nsub, a.ntr);
     if (wc) k_interp_sm_wc<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
-    else k_interp_sm<T, DIM, NS><<<grid, kInterpThreads, sm, s>>>(a, gmap, tma);
+    else k_interp_sm<T, DIM, NS><<<grid, interp_threads<T>(), sm, s>>>(a, gmap, tma);
   }
   return cudaGetLastError();
 }
