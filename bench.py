@@ -476,17 +476,16 @@ def _tuned_plan(w: Workload, dev, stream, opts, pts_dev, args_ce, flush, tuned: 
             alt.set_pts(*pts_dev[::-1])
         torch.cuda.synchronize()
         best = alt.autotune()[0]
-        if (best["method"], best["binsizex"], best["binsizey"], best["binsizez"]) != (
-                selector_info["method"], selector_info["binsizex"], selector_info["binsizey"],
-                selector_info["binsizez"]):
-            k = 3
-            for p in (plan, alt):
-                _time_device(p, args_ce, 1, stream, flush)
-            t_sel = _time_device(plan, args_ce, k, stream, flush)
-            t_alt = _time_device(alt, args_ce, k, stream, flush)
-            if t_alt < t_sel:
-                plan, alt = alt, plan
-                tune = best
+        # always timed against each other: plan info does not report the
+        # subproblem cap, so equal method and bins can still be two classes
+        k = 3
+        for p in (plan, alt):
+            _time_device(p, args_ce, 1, stream, flush)
+        t_sel = _time_device(plan, args_ce, k, stream, flush)
+        t_alt = _time_device(alt, args_ce, k, stream, flush)
+        if t_alt < t_sel:
+            plan, alt = alt, plan
+            tune = best
         del alt
     return plan, tune, selector_info
 

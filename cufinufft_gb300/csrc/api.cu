@@ -1936,9 +1936,13 @@ static int time_stage(Plan<T>* p, cplx_t<T>* scratch, cplx_t<T>* grid, int reps,
 // 3-8 method 2 with small / medium / large bins x subproblem cap 256 / 1024,
 // 9-11 method 5 (cell-run spread, type 1) with small / medium / large bins.
 // Bin shapes per dimension: 1D 256 / 1024 / 4096; 2D 16^2 / 32^2 / 64^2;
-// 3D 8x8x8 / 16x16x2 / 16x16x4 (clamped to the fine grid).  A class the plan
-// cannot run (method 2 for 1D type 2, method 5 for type 2 or past its
-// limits, a tile beyond shared memory) has ms = -2.
+// 3D 8x8x8 / 16x16x2 / 16x16x4 (clamped to the fine grid); for FP64 3D
+// plans the large shape is 16x16xbz with the largest bz of 8, 6, 4 whose
+// FP64 tile fits shared memory: at ns 11 a 16x16x8 bin holds ~16x the
+// points of an 8^3 bin for 2x the tile, and interpolation on clustered 3D
+// points at tol 1e-9 ran 24.5 ms (8^3) against 11.4 ms (16x16x8).  A class
+// the plan cannot run (method 2 for 1D type 2, method 5 for type 2 or past
+// its limits, a tile beyond shared memory) has ms = -2.
 constexpr int kLayoutClasses = 12;
 
 template <typename T>
@@ -1949,7 +1953,16 @@ static cufinufft_tune_entry layout_class(const Plan<T>* p, int cls) {
   cufinufft_tune_entry e;
   e.method = cls < 3 ? 1 : (cls < 9 ? 2 : 5);
   const int shape = cls < 3 ? cls : (cls < 9 ? (cls - 3) / 2 : cls - 9);
-  const int* sh = shapes[p->dim - 1][shape];
+  int sh[3] = {shapes[p->dim - 1][shape][0], shapes[p->dim - 1][shape][1], shapes[p->dim - 1][shape][2]};
+  if (sizeof(T) == 8 && p->dim == 3 && shape == 2) {
+    for (int bz : {8, 6, 4}) {
+      const int b3[3] = {16, 16, bz};
+      if (tile_cells(3, p->sp.ns, b3) * sizeof(cplx_t<T>) <= (size_t)max_smem_optin(p->device)) {
+        sh[2] = bz;
+        break;
+      }
+    }
+  }
   e.binsizex = std::min(sh[0], p->nf[0]);
   e.binsizey = p->dim > 1 ? std::min(sh[1], p->nf[1]) : 1;
   e.binsizez = p->dim > 2 ? std::min(sh[2], p->nf[2]) : 1;

@@ -37,16 +37,20 @@ constexpr int kSpreadThreads = 256;
 // Threads of a k_interp_sm block, and the blocks per SM its register bound
 // is set for.  FP32: 256 threads, 6 blocks (40 registers a thread for
 // ns <= 9; 4 blocks above).  FP64 plans' subproblem interpolation (FP64 or
-// double-float): 512 threads, one block, the same 128 registers a thread as
-// two 256-thread blocks (which ran radial 2D FP64 at ns 13 4% faster than one
-// block of 188 registers, despite 52 bytes of spill); measured at ns 14, the
-// double-float kernel 1.11 -> 1.01 ms with 512-thread blocks, while FP32 plans
-// keep 256 (34.2 vs 35.1 us at ns 8).
+// double-float), 128 registers a thread (two 256-thread blocks ran radial 2D
+// FP64 at ns 13 4% faster than one block of 188 registers, despite 52 bytes
+// of spill): 2D in one 512-thread block -- the double-float kernel on radial
+// 2D at ns 14 1.11 -> 1.01 ms -- and 3D in two 256-thread blocks, whose
+// sparse subproblems (tens of points per 8^3 bin) leave most of a 512-thread
+// block idle (clustered 3D at ns 11: 74.3 ms against 79.4 ms).  FP32 plans
+// keep 256-thread blocks (34.2 vs 35.1 us at ns 8).
 constexpr int kInterpThreads = 256;
 constexpr int kInterpBlocksF32 = 6 * 256 / kInterpThreads;
-constexpr int kInterpThreadsF64 = 512;
-constexpr int kInterpBlocksF64 = 1;
-template <typename T> constexpr int interp_threads() { return sizeof(T) == 4 ? kInterpThreads : kInterpThreadsF64; }
+template <int DIM> constexpr int interp_threads_f64() { return DIM == 2 ? 512 : 256; }
+template <int DIM> constexpr int interp_blocks_f64() { return DIM == 2 ? 1 : 2; }
+template <typename T, int DIM> constexpr int interp_threads() {
+  return sizeof(T) == 4 ? kInterpThreads : interp_threads_f64<DIM>();
+}
 
 // Subproblem header shared by the shared-memory kernels.
 struct SubTile {
@@ -553,7 +557,7 @@ struct InterpPoint {
 // wait: evaluated before it, the rows stay live across the wait and the FP32
 // kernels spill at the 40-register bound (measured 3.5% slower).
 template <typename T, int DIM, int NS>
-__global__ void __launch_bounds__(interp_threads<T>(), sizeof(T) == 4 ? (NS <= 9 ? kInterpBlocksF32 : kInterpBlocksF32 * 2 / 3) : kInterpBlocksF64)
+__global__ void __launch_bounds__(interp_threads<T, DIM>(), sizeof(T) == 4 ? (NS <= 9 ? kInterpBlocksF32 : kInterpBlocksF32 * 2 / 3) : interp_blocks_f64<DIM>())
 k_interp_sm(SpreadArgs<T> a, const __grid_constant__ CUtensorMap gmap, int tma) {
   using C = cplx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -642,7 +646,7 @@ __device__ __forceinline__ DF df_kernel_tap(double d, int j, const KernelCoeffs<
 }
 
 template <int DIM, int NS>
-__global__ void __launch_bounds__(kInterpThreadsF64, kInterpBlocksF64)
+__global__ void __launch_bounds__(interp_threads_f64<DIM>(), interp_blocks_f64<DIM>())
 k_interp_sm_df(SpreadArgs<double> a, const __grid_constant__ CUtensorMap gmap, int tma) {
   using C = double2;
   constexpr int HD = horner_degree<double>(NS);
@@ -1893,7 +1897,7 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
       if (!wc && a.fp64_df) {
         cudaError_t e = prepare_smem(k_interp_sm_df<DIM, NS>, sm);
         if (e != cudaSuccess) return e;
-        k_interp_sm_df<DIM, NS><<<dim3(a.bins.nsub, a.ntr), kInterpThreadsF64, sm, s>>>(a, gmap, tma);
+        k_interp_sm_df<DIM, NS><<<dim3(a.bins.nsub, a.ntr), interp_threads_f64<DIM>(), sm, s>>>(a, gmap, tma);
         return cudaGetLastError();
       }
     }
@@ -1902,7 +1906,7 @@ cudaError_t interp_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     dim3 grid(a.bins.nsub, a.ntr);
     if (wc) k_interp_sm_wc<T, DIM, NS><<<grid, kSpreadThreads, sm, s>>>(a);
-    else k_interp_sm<T, DIM, NS><<<grid, interp_threads<T>(), sm, s>>>(a, gmap, tma);
+    else k_interp_sm<T, DIM, NS><<<grid, interp_threads<T, DIM>(), sm, s>>>(a, gmap, tma);
   }
   return cudaGetLastError();
 }
