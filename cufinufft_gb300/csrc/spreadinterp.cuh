@@ -952,18 +952,19 @@ k_spread_sm_wc(SpreadArgs<T> a) {
 // NS warps and warp w alone writes the planes z = w (mod NS).  A point's
 // support covers NS consecutive planes, one of each residue, so every warp
 // handles exactly one plane of every point, and it adds the point's NS x NS
-// taps there with plain shared loads and stores: lanes over (x, y) taps, R =
-// 32 / NS rows per instruction, distinct cells, and a __syncwarp between
-// points, which orders one point's stores before the next point's loads.
-// The block stages the kernel values of CH points at a time (c kx as
-// complex, ky, kz, the point's tile offset) in a double buffer, one block
-// barrier per chunk.  Rows are padded to a pitch PX = -NS (mod 32), so the R
-// rows of an instruction fall in disjoint banks.  Results equal the atomic
-// kernels' up to the order of additions.
+// taps there with plain shared loads and stores of complex cells: lanes over
+// (x, y) taps, R = 32 / NS rows per instruction, distinct cells, and a
+// __syncwarp between points, which orders one point's stores before the next
+// point's loads.  The block stages the kernel values of CH points at a time
+// (c kx as complex, ky, kz, the point's tile offset) in a double buffer, one
+// block barrier per chunk.  Rows are padded to a pitch PX = NS (mod 16)
+// complex cells, so lane l's cell is l (mod 16): the rows of one instruction
+// fall in distinct banks.  Results equal the atomic kernels' up to the order
+// of additions.
 constexpr int kSlabChunk = 64;
 
 __host__ __device__ constexpr int slab_pitch(int tx, int ns) {
-  return tx + (((32 - ns - tx) % 32) + 32) % 32;
+  return tx + (((ns - tx) % 16) + 16) % 16;
 }
 
 template <typename T>
@@ -971,7 +972,28 @@ size_t slab_bytes(int ns, const BinTables& bt) {
   const size_t px = slab_pitch(bt.bs[0] + ns - 1, ns);
   const size_t cells = px * (bt.bs[1] + ns - 1) * (bt.bs[2] + ns - 1);
   const size_t stage = (size_t)kSlabChunk * ns * (sizeof(cplx_t<T>) + 2 * sizeof(T)) + kSlabChunk * sizeof(int2);
-  return cells * 2 * sizeof(T) + 16 + 2 * stage;  // stage aligned to 16 bytes
+  return cells * sizeof(cplx_t<T>) + 16 + 2 * stage;  // stage aligned to 16 bytes
+}
+
+// Flush of an interleaved complex tile with row pitch `pitch` (cells).
+template <typename T>
+__device__ __forceinline__ void cplx_flush(const cplx_t<T>* tile, cplx_t<T>* grid, const SubTile& st,
+                                           const GridGeom& g, int pitch) {
+  const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
+  const int rows = st.TY * st.TZ;
+  TileRows rw(threadIdx.x >> 5, st.TY);
+  const bool inside = tile_in_grid(st, g);
+  for (int r = threadIdx.x >> 5; r < rows; r += nwb, rw.next(nwb, st.TY)) {
+    const int gy = inside ? st.oy + rw.iy : wrap3(st.oy + rw.iy, g.nf[1]);
+    const int gz = inside ? st.oz + rw.iz : wrap3(st.oz + rw.iz, g.nf[2]);
+    cplx_t<T>* dst = grid + ((size_t)gz * g.nf[1] + gy) * g.nf[0];
+    const cplx_t<T>* src = tile + (size_t)r * pitch;
+    for (int ix = lane; ix < st.TX; ix += 32) {
+      const cplx_t<T> v = src[ix];
+      if (v.x == T(0) && v.y == T(0)) continue;
+      red_add(dst + (inside ? st.ox + ix : wrap3(st.ox + ix, g.nf[0])), v.x, v.y);
+    }
+  }
 }
 
 template <typename T, int NS>
@@ -995,14 +1017,13 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
   const int PX = slab_pitch(st.TX, NS);
   const int PP = PX * st.TY;                  // plane stride
   const int ncell = PP * st.TZ;
-  T* re = reinterpret_cast<T*>(smem_raw);
-  T* im = re + ncell;
+  C* tile = reinterpret_cast<C*>(smem_raw);
   // double-buffered stage: [c kx (complex) | ky | kz] x CH x NS, then
   // (tile offset, lz mod NS) per point
-  unsigned char* stage0 = smem_raw + ((2 * (size_t)ncell * sizeof(T) + 15) & ~(size_t)15);
+  unsigned char* stage0 = smem_raw + (((size_t)ncell * sizeof(C) + 15) & ~(size_t)15);
   const size_t stage_sz = (size_t)CH * NS * (sizeof(C) + 2 * sizeof(T)) + CH * sizeof(int2);
   const int t = blockIdx.y;
-  for (int i = threadIdx.x; i < 2 * ncell; i += blockDim.x) re[i] = T(0);
+  for (int i = threadIdx.x; i < ncell; i += blockDim.x) tile[i] = C{T(0), T(0)};
   const C* cin = a.c_in + (size_t)t * a.M;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int dx = lane % NS, dyl = lane / NS;
@@ -1042,42 +1063,38 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
         const int dy = r * R + dyl;
         if (kFullRows || (lane_on && dy < NS)) {
           const T ky = s_ky[q * NS + dy];
-          const int o = base + dy * PX;
-          re[o] = fma_rn(ur, ky, re[o]);
-          im[o] = fma_rn(ui, ky, im[o]);
+          C v = tile[base + dy * PX];
+          v.x = fma_rn(ur, ky, v.x);
+          v.y = fma_rn(ui, ky, v.y);
+          tile[base + dy * PX] = v;
         }
       }
       __syncwarp();  // this point's stores before the next point's loads
     }
   }
   __syncthreads();
-  plane_flush<T>(re, im, a.fw + (size_t)t * a.g.Nf, st, a.g, PX);
+  cplx_flush<T>(tile, a.fw + (size_t)t * a.g.Nf, st, a.g, PX);
 }
 
 // ---------------------------------------------------------------------------
 // Private-tile 2D spreading (method 2, the default for 2D subproblems).  A 2D
 // tile is small (39 x 40 cells at ns 8 with 32 x 32 bins), so each of the
 // block's kPrivWarps warps accumulates its share of the subproblem's points
-// into a private copy with plain shared loads and stores -- lanes over the
-// point's (x, y) taps, 32 / NS rows per instruction, a __syncwarp between
-// points -- and the copies are summed cell by cell once at the end (one
-// thread per cell, no atomics) and flushed.  Each warp stages the kernel rows
-// of 32 points at a time in warp-private shared memory (c kx as complex, ky,
-// the tile offset): lane q evaluates point q's rows.  Rows are padded to a
-// pitch of +-NS (mod 32), so the rows of one instruction fall in disjoint
-// banks.  Results equal the atomic kernel's up to the order of additions.
+// into a private copy of complex cells with plain shared loads and stores --
+// lanes over the point's (x, y) taps, 32 / NS rows per instruction, a
+// __syncwarp between points -- and the copies are summed cell by cell once at
+// the end (one thread per cell, no atomics) and flushed.  Each warp stages
+// the kernel rows of 32 points at a time in warp-private shared memory (c kx
+// as complex, ky, the tile offset): lane q evaluates point q's rows.  Rows
+// are padded to the slab kernel's pitch (NS mod 16 cells), so the rows of one
+// instruction fall in distinct banks.  Results equal the atomic kernel's up
+// to the order of additions.
 constexpr int kPrivWarps = 4;
-
-__host__ __device__ constexpr int priv_pitch(int tx, int ns) {
-  // smallest pitch >= tx that is ns or 32 - ns (mod 32)
-  return ((tx % 32) <= ns) ? tx + (ns - tx % 32) : ((tx % 32) <= 32 - ns ? tx + (32 - ns - tx % 32)
-                                                                         : tx + (32 - tx % 32) + ns);
-}
 
 template <typename T>
 size_t priv_bytes(int ns, const BinTables& bt) {
-  const size_t px = priv_pitch(bt.bs[0] + ns - 1, ns);
-  const size_t copy = px * (bt.bs[1] + ns - 1) * 2 * sizeof(T);          // re and im planes
+  const size_t px = slab_pitch(bt.bs[0] + ns - 1, ns);
+  const size_t copy = px * (bt.bs[1] + ns - 1) * sizeof(cplx_t<T>);
   const size_t stage = 32 * (size_t)ns * (sizeof(cplx_t<T>) + sizeof(T)) + 32 * sizeof(int);
   return kPrivWarps * (((copy + 15) & ~(size_t)15) + ((stage + 15) & ~(size_t)15));
 }
@@ -1097,18 +1114,17 @@ k_spread_sm_priv(SpreadArgs<T> a, int split) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const SubTile st = sub_tile_block<2, NS>(a.bins, blockIdx.x);
   if (first >= st.np) return;  // block-uniform
-  const int PX = priv_pitch(st.TX, NS);
+  const int PX = slab_pitch(st.TX, NS);
   const int ncell = PX * st.TY;
-  const size_t copy_sz = ((size_t)ncell * 2 * sizeof(T) + 15) & ~(size_t)15;
+  const size_t copy_sz = ((size_t)ncell * sizeof(C) + 15) & ~(size_t)15;
   const size_t stage_sz = ((size_t)32 * NS * (sizeof(C) + sizeof(T)) + 32 * sizeof(int) + 15) & ~(size_t)15;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T* re = reinterpret_cast<T*>(smem_raw + warp * copy_sz);
-  T* im = re + ncell;
+  C* tile = reinterpret_cast<C*>(smem_raw + warp * copy_sz);
   unsigned char* sb = smem_raw + kPrivWarps * copy_sz + warp * stage_sz;
   C* s_ck = reinterpret_cast<C*>(sb);
   T* s_ky = reinterpret_cast<T*>(s_ck + 32 * NS);
   int* s_base = reinterpret_cast<int*>(s_ky + 32 * NS);
-  for (int i = lane; i < 2 * ncell; i += 32) re[i] = T(0);
+  for (int i = lane; i < ncell; i += 32) tile[i] = C{T(0), T(0)};
   const int t = blockIdx.y;
   const C* cin = a.c_in + (size_t)t * a.M;
   const int dx = lane % NS, dyl = lane / NS;
@@ -1167,9 +1183,10 @@ k_spread_sm_priv(SpreadArgs<T> a, int split) {
       for (int r = 0; r < NR; ++r) {
         const int dy = r * R + dyl;
         if (kFullRows || (lane_on && dy < NS)) {
-          const int o = base + dy * PX;
-          re[o] = fma_rn(ck.x, ky[r], re[o]);
-          im[o] = fma_rn(ck.y, ky[r], im[o]);
+          C v = tile[base + dy * PX];
+          v.x = fma_rn(ck.x, ky[r], v.x);
+          v.y = fma_rn(ck.y, ky[r], v.y);
+          tile[base + dy * PX] = v;
         }
       }
       __syncwarp();  // this point's stores before the next point's loads
@@ -1181,21 +1198,19 @@ k_spread_sm_priv(SpreadArgs<T> a, int split) {
   }
   __syncthreads();
   // sum the private copies into copy 0, one thread per cell
-  T* re0 = reinterpret_cast<T*>(smem_raw);
-  T* im0 = re0 + ncell;
+  C* tile0 = reinterpret_cast<C*>(smem_raw);
   for (int i = threadIdx.x; i < ncell; i += blockDim.x) {
-    T sr = re0[i], si = im0[i];
+    C sum = tile0[i];
 #pragma unroll
     for (int w = 1; w < kPrivWarps; ++w) {
-      const T* rw = reinterpret_cast<const T*>(smem_raw + w * copy_sz);
-      sr += rw[i];
-      si += rw[i + ncell];
+      const C v = reinterpret_cast<const C*>(smem_raw + w * copy_sz)[i];
+      sum.x += v.x;
+      sum.y += v.y;
     }
-    re0[i] = sr;
-    im0[i] = si;
+    tile0[i] = sum;
   }
   __syncthreads();
-  plane_flush<T>(re0, im0, a.fw + (size_t)t * a.g.Nf, st, a.g, PX);
+  cplx_flush<T>(tile0, a.fw + (size_t)t * a.g.Nf, st, a.g, PX);
 }
 
 // CUFINUFFT_SPREAD_PRIV=0: 2D subproblem spreading by the warp-cooperative
