@@ -861,8 +861,8 @@ k_spread_gm_wc(SpreadArgs<T> a) {
 // other bank of 2 ns (interleaved complex), halving bank conflicts.
 template <typename T>
 __device__ __forceinline__ void plane_flush(const T* re, const T* im, cplx_t<T>* grid,
-                                            const SubTile& st, const GridGeom& g, int pitch = 0) {
-  if (pitch == 0) pitch = st.TX;  // row pitch of the planes (elements)
+                                            const SubTile& st, const GridGeom& g) {
+  const int pitch = st.TX;  // row pitch of the planes (elements)
   const int lane = threadIdx.x & 31, nwb = blockDim.x >> 5;
   const int rows = st.TY * st.TZ;
   TileRows rw(threadIdx.x >> 5, st.TY);
