@@ -109,3 +109,18 @@ def test_priv_spread_clustered_full_subproblems(monkeypatch):
     ref = NC.oracle_nufft(1, modes, [p.astype(np.float64) for p in pts], c, 1e-5, True,
                           gpu_method=2)
     assert _rel(out, ref) < 2e-5
+
+
+def test_priv_falls_back_when_it_does_not_fit():
+    """FP64 at ns 16 with 64^2 bins: four private copies of the tile exceed
+    shared memory, so the launch takes the atomic kernel -- results against
+    the oracle."""
+    rng = np.random.default_rng(32)
+    modes, M = (80, 72), 20000
+    pts = NC.points(rng, 2, M, dtype=np.float64, edges=False)
+    c = NC.strengths(rng, M)
+    out, info = NC.run_gpu(1, modes, pts, c, 1e-15, False, gpu_method=2, gpu_binsizex=64,
+                           gpu_binsizey=64)
+    assert info["ns"] == 16
+    ref = NC.oracle_nufft(1, modes, pts, c, 1e-15, False, gpu_method=2)
+    assert _rel(out, ref) < 1e-10, info

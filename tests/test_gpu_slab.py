@@ -112,3 +112,18 @@ def test_slab_spread_clustered_full_subproblems(monkeypatch):
     ref = NC.oracle_nufft(1, modes, [p.astype(np.float64) for p in pts], c, 1e-5, True,
                           gpu_method=2)
     assert _rel(out, ref) < 2e-5
+
+
+def test_slab_falls_back_when_it_does_not_fit():
+    """FP64 at ns 16 with 8^3 bins: the tile fits shared memory but the
+    slab kernel's padded tile and staging do not, so the launch takes the
+    atomic kernel -- results against the oracle."""
+    rng = np.random.default_rng(31)
+    modes, M = (20, 18, 16), 6000
+    pts = NC.points(rng, 3, M, dtype=np.float64, edges=False)
+    c = NC.strengths(rng, M)
+    out, info = NC.run_gpu(1, modes, pts, c, 1e-15, False, gpu_method=2, gpu_binsizex=8,
+                           gpu_binsizey=8, gpu_binsizez=8)
+    assert info["ns"] == 16
+    ref = NC.oracle_nufft(1, modes, pts, c, 1e-15, False, gpu_method=2)
+    assert _rel(out, ref) < 1e-10, info
