@@ -15,11 +15,18 @@ template <> struct cplx<float> { using type = float2; };
 template <> struct cplx<double> { using type = double2; };
 template <typename T> using cplx_t = typename cplx<T>::type;
 
-// Degree of the fitted piecewise polynomials (kerevalmeth 1).  The fit error
-// reaches the kernel's own truncation level exp(-beta) ~ 10^-ns by degree
-// ns+1 (FP32) and ns+2 (FP64); one more degree is kept as margin.
+// Degree of the fitted piecewise polynomials (kerevalmeth 1).  FP32: ns + 2.
+// FP64: the least degree at which the fit error (relative to the kernel's
+// peak, over every tap interval) comes within 1.5x of its floor -- the
+// kernel's own truncation level, ~exp(-beta) -- plus one as margin.  Measured
+// with the fit's Chebyshev construction at upsampfac 2 (the upsampfac 1.25
+// kernels need at most the same): the least degree is ns + 1 for ns <= 6,
+// ns for 7-8, ns - 1 for 9-12, ns - 2 for 13-14 and ns - 3 for 15-16, so
+// wide FP64 kernels evaluate 4 to 6 fewer Horner steps per value than with
+// degree ns + 3.
 template <typename T> constexpr int horner_degree(int ns) {
-  return sizeof(T) == 4 ? ns + 2 : ns + 3;
+  constexpr int kDegF64[17] = {0, 0, 4, 5, 6, 7, 8, 8, 9, 9, 10, 11, 12, 12, 13, 13, 13};
+  return sizeof(T) == 4 ? ns + 2 : kDegF64[ns < 2 ? 2 : (ns > 16 ? 16 : ns)];
 }
 
 // Constants that place one coordinate axis on the fine grid (see
