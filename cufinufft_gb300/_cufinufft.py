@@ -73,7 +73,8 @@ class PlanInfo(ctypes.Structure):
         "nsubprob", "kerevalmeth")] + [("beta", c_double), ("es_c", c_double),
                                        ("line_fft", c_int), ("cell_order", c_int),
                                        ("width_rule", c_int), ("chain_fp32", c_int),
-                                       ("half_fft", c_int), ("fp64_df", c_int)]
+                                       ("half_fft", c_int), ("fp64_df", c_int),
+                                       ("df_fft", c_int)]
 
 
 CufinufftPlan = c_void_p

@@ -157,6 +157,13 @@ template <typename T> static void release(Plan<T>* p) {
   }
   p->line_fft = false;
   p->half_fft = false;
+  p->df_fft = false;
+  cudaFree(p->df_tmp);
+  p->df_tmp = nullptr;
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(p->df_tw[k]);
+    p->df_tw[k] = nullptr;
+  }
   p->horner.clear();
   cudaFree(p->sel_buf);
   p->sel_buf = nullptr;
@@ -249,6 +256,57 @@ static bool use_half_fft(const Plan<T>* p) {
   for (int k = 0; k < p->dim; ++k)
     if (!half_fft_size_ok(p->nf[k]) || 2 * p->N[k] > p->nf[k]) return false;
   return true;
+}
+
+// Double-float FFT (fft_df.cu) for FP64 plans of dimension 2 whose fine
+// grid sides are powers of two <= 4096, when the tol gate allows it and no
+// other FFT form was asked for.
+template <typename T>
+static bool use_df_fft(const Plan<T>* p) {
+  if (sizeof(T) != 8 || !p->df_fft_ok || p->dim != 2 || (p->type != 1 && p->type != 2)) return false;
+  if (std::getenv("CUFINUFFT_FFT")) return false;  // line / half forms asked for
+  return fft_df_size_ok(p->nf[0]) && fft_df_size_ok(p->nf[1]);
+}
+
+// Its scratch grids and, per axis, W^k = exp(iflag 2 pi i k / nf), k < nf/2,
+// computed in extended precision and split into float pairs.
+template <typename T>
+static int make_df_fft(Plan<T>* p) {
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  const size_t Nf = (size_t)p->nf[0] * p->nf[1];
+  CFG_CUDA(cudaMalloc(&p->df_tmp, sizeof(double2) * Nf * p->maxbatch));
+  for (int k = 0; k < 2; ++k) {
+    const int n = p->nf[k];
+    std::vector<float4> h((size_t)n / 2);
+    for (int m = 0; m < n / 2; ++m) {
+      const long double a = two_pi * (long double)m / (long double)n * (p->iflag >= 0 ? 1 : -1);
+      const double re = (double)cosl(a), im = (double)sinl(a);
+      const float rh = (float)re, ih = (float)im;
+      h[m] = make_float4(rh, (float)(re - (double)rh), ih, (float)(im - (double)ih));
+    }
+    CFG_CUDA(cudaMalloc(&p->df_tw[k], sizeof(float4) * h.size()));
+    CFG_CUDA(cudaMemcpyAsync(p->df_tw[k], h.data(), sizeof(float4) * h.size(), cudaMemcpyHostToDevice,
+                             p->stream));
+  }
+  CFG_CUDA(cudaStreamSynchronize(p->stream));
+  return 0;
+}
+
+// 2D transform of B grids in -> out through the scratch: rows along x, a
+// transpose, rows along y, a transpose back.  in may equal out (type 1).
+template <typename T>
+static cudaError_t df_fft_exec(Plan<T>* p, const cplx_t<T>* in, cplx_t<T>* out, int B) {
+  if constexpr (sizeof(T) == 8) {
+    const int nx = p->nf[0], ny = p->nf[1];
+    cudaError_t e = launch_fft_df_rows(in, p->df_tmp, nx, (long long)B * ny, p->df_tw[0], p->stream);
+    if (e == cudaSuccess) e = launch_transpose_d2(p->df_tmp, out, ny, nx, B, p->stream);
+    if (e == cudaSuccess) e = launch_fft_df_rows(out, p->df_tmp, ny, (long long)B * nx, p->df_tw[1], p->stream);
+    if (e == cudaSuccess) e = launch_transpose_d2(p->df_tmp, out, nx, ny, B, p->stream);
+    return e;
+  } else {
+    (void)p; (void)in; (void)out; (void)B;
+    return cudaErrorInvalidValue;
+  }
 }
 
 // Twiddle tables W^m = exp(iflag 2 pi i m / nf_d), m < nf_d, per axis, in
@@ -747,6 +805,14 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
       p->fp64_df = v && v[0] == '0' ? 0 : (v && v[0] == '1' ? 1 : (tol >= 1e-13 ? 1 : 0));
     }
   }
+  if constexpr (sizeof(T) == 8) {
+    // double-float FFT of 2D power-of-two grids (types 1 and 2), under the
+    // same tol gate; CUFINUFFT_FP64_DF_FFT=0 keeps cuFFT's Z2Z
+    const char* v = std::getenv("CUFINUFFT_FP64_DF_FFT");
+    const char* w = std::getenv("CUFINUFFT_FP64_DF");
+    const bool gate = w && w[0] == '0' ? false : (w && w[0] == '1' ? true : tol >= 1e-13);
+    p->df_fft_ok = (v && v[0] == '0') ? 0 : (gate ? 1 : 0);
+  }
 
   const long long Nf = grid_cells(p);
   CFG_CUDA(cudaMalloc(&p->count, sizeof(int) * (size_t)p->nbins));
@@ -772,7 +838,18 @@ static int makeplan_impl(Plan<T>* p, int type, int dim, const int* nmodes, int i
   for (int k = 0; k < dim; ++k) CFG_CUDA(cudaMalloc(&p->fac[k], sizeof(T) * (size_t)p->N[k]));
 
   int e = 0;
-  if (use_half_fft(p)) {
+  if (use_df_fft(p)) {
+    // double-float FFT: no cuFFT plan; scratch for the passes, twiddles per axis
+    e = make_df_fft(p);
+    if (e) return e;
+    if (type == 2) {
+      // as with cuFFT: fw holds only the amplified modes over zero padding,
+      // the transform writes fw2, interpolation reads fw2
+      CFG_CUDA(cudaMalloc(&p->fw2, sizeof(cplx_t<T>) * (size_t)Nf * p->maxbatch));
+      CFG_CUDA(cudaMemsetAsync(p->fw, 0, sizeof(cplx_t<T>) * (size_t)Nf * p->maxbatch, p->stream));
+    }
+    p->df_fft = true;
+  } else if (use_half_fft(p)) {
     // pruned power-of-two passes: no cuFFT plan; type 2 grid in fw2
     // (intermediates in fw), type 1 intermediates in fw2
     e = make_twiddles(p);
@@ -1107,7 +1184,8 @@ static int execute_direct(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
           CFG_CUDA(launch_line_fft<T>(passes[i], p->stream));
         }
       } else {
-        CFG_CUFFT(fft_exec(h, p->fw, p->iflag));
+        if (p->df_fft) CFG_CUDA(df_fft_exec(p, p->fw, p->fw, B));
+        else CFG_CUFFT(fft_exec(h, p->fw, p->iflag));
         mark(p, ev[2]);
         CFG_CUDA(launch_deconvolve<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
                                       p->fac[1], p->fac[2], B, p->stream));
@@ -1131,7 +1209,8 @@ static int execute_direct(Plan<T>* p, cplx_t<T>* c, cplx_t<T>* fk) {
         CFG_CUDA(launch_amplify_modes<T>(p->dim, p->nf, p->N, p->fw, fk + (size_t)b0 * Nm, p->fac[0],
                                          p->fac[1], p->fac[2], B, p->stream));
         mark(p, ev[1]);
-        CFG_CUFFT(fft_exec(h, p->fw, p->fw2, p->iflag));
+        if (p->df_fft) CFG_CUDA(df_fft_exec(p, p->fw, p->fw2, B));
+        else CFG_CUFFT(fft_exec(h, p->fw, p->fw2, p->iflag));
         mark(p, ev[2]);
       }
       a.fw_in = p->fw2 ? p->fw2 : p->fw;
@@ -1707,6 +1786,7 @@ static void fill_info(const Plan<T>* p, cufinufft_plan_info* info) {
   info->es_c = p->sp.c;
   info->line_fft = p->line_fft ? 1 : 0;
   info->half_fft = p->half_fft ? 1 : 0;
+  info->df_fft = p->df_fft ? 1 : 0;
   info->fp64_df = p->fp64_df && p->method == 2 ? 1 : 0;  // the subproblem interpolation only
   info->cell_order = p->cell_order ? 1 : 0;
   info->width_rule = p->width_rule;

@@ -255,6 +255,16 @@ struct HalfPass {
 };
 template <typename T> cudaError_t launch_half_pass(const HalfPass<T>& a, cudaStream_t s);
 bool half_fft_size_ok(int nf);
+
+// Double-float FFT of FP64 grids (fft_df.cu): 1D transforms of length n (a
+// power of two <= 4096) over `rows` consecutive rows, twiddles tw[k] =
+// exp(sign 2 pi i k / n), k < n/2, as float pairs (re hi, re lo, im hi,
+// im lo); and the batched transpose of R x C planes of double2.
+bool fft_df_size_ok(int n);
+size_t fft_df_smem(int n);
+cudaError_t launch_fft_df_rows(const double2* in, double2* out, int n, long long rows, const float4* tw,
+                               cudaStream_t s);
+cudaError_t launch_transpose_d2(const double2* in, double2* out, int R, int C, int batch, cudaStream_t s);
 int half_fft_mp(int nf);
 // Pitch of the column buffers of the strided passes for n values per column
 // and Mp-point transforms (at least both, bank-conflict offset added).

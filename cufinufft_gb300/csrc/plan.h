@@ -43,6 +43,11 @@ template <typename T> struct Plan {
   // exp(iflag 2 pi i m / nf_d) and radix sequences
   bool line_fft = false;
   bool half_fft = false;  // pruned power-of-two passes (halffft.cu), tables in tw
+  // FP64 2D grids: double-float FFT (fft_df.cu) instead of cuFFT's Z2Z
+  bool df_fft = false;
+  int df_fft_ok = 0;            // set at makeplan: precision, tol and switch allow it
+  double2* df_tmp = nullptr;    // maxbatch grids of scratch
+  float4* df_tw[2] = {nullptr, nullptr};  // twiddles per axis (float pairs)
   C* tw[3] = {nullptr, nullptr, nullptr};
   std::vector<int> rad[3];
   int rem = 0;

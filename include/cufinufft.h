@@ -113,6 +113,7 @@ typedef struct cufinufft_plan_info {
   int chain_fp32; /* 1: an FP64 plan running its spread/interp, FFT and deconvolution in FP32 */
   int half_fft;   /* 1: pruned power-of-two FFT passes (halffft.cu) instead of cuFFT */
   int fp64_df;    /* 1: an FP64 type-2 method-2 plan interpolating in double-float (FP32 pairs) */
+  int df_fft;     /* 1: an FP64 2D plan transforming its grid in double-float (fft_df.cu) */
 } cufinufft_plan_info;
 int cufinufft_get_info(cufinufft_plan plan, cufinufft_plan_info* info);
 int cufinufftf_get_info(cufinufftf_plan plan, cufinufft_plan_info* info);
