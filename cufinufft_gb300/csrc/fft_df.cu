@@ -21,7 +21,11 @@
 namespace cfg {
 namespace {
 
-constexpr int kFftDfThreads = 256;
+// 512 threads: three blocks of 64 KB (n = 2048) per SM keep 48 warps
+// resident, which the double-float butterflies' latency chains need
+// (radial 2D FP64, 2048^2: 384 -> 350 us with the first stage below; a
+// radix-4 form of the stages measured slower, 376 us)
+constexpr int kFftDfThreads = 512;
 
 __device__ __forceinline__ float4 split_c(double2 v) {
   const DF r = df_from(v.x), i = df_from(v.y);
@@ -46,7 +50,22 @@ k_fft_df_rows(const double2* __restrict__ in, double2* __restrict__ out, int n, 
   for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = split_c(src[i]);
   __syncthreads();
   const int half = n >> 1;
-  for (int Ns = 1; Ns < n; Ns <<= 1) {
+  // first stage: every twiddle is 1
+  for (int j = threadIdx.x; j < half; j += blockDim.x) {
+    const float4 a = x[j], b = x[j + half];
+    const DF ar{a.x, a.y}, ai{a.z, a.w}, br{b.x, b.y}, bi{b.z, b.w};
+    const DF s0r = df_add(ar, br), s0i = df_add(ai, bi);
+    const DF s1r = df_add(ar, dneg(br)), s1i = df_add(ai, dneg(bi));
+    y[2 * j] = make_float4(s0r.h, s0r.l, s0i.h, s0i.l);
+    y[2 * j + 1] = make_float4(s1r.h, s1r.l, s1i.h, s1i.l);
+  }
+  __syncthreads();
+  {
+    float4* t = x;
+    x = y;
+    y = t;
+  }
+  for (int Ns = 2; Ns < n; Ns <<= 1) {
     const int tstep = half / Ns;  // twiddle index = (j mod Ns) * n / (2 Ns)
     for (int j = threadIdx.x; j < half; j += blockDim.x) {
       const float4 a = x[j], b = x[j + half];
