@@ -1232,15 +1232,17 @@ inline bool slab_spread_enabled() {
 // its own).  setpts sorts a bin's points by first-tap cell, so dense regions
 // arrive as long runs of points that all add into the same ns^d cells.  A
 // warp walks its slice of the subproblem in chunks of 32 points.  A chunk
-// whose points share one cell is summed in registers -- lane l takes the
-// taps l, l + 32, ..., four at a time -- from the points' kernel values
-// staged in warp-private shared memory, then each tap sum is added to the
-// tile once (conflict-free: the lanes' taps differ).  Any other chunk is
-// spread point by point with shared atomics, lanes over x taps as in
-// k_spread_sm_wc.  Dense chunks thus cost FMAs instead of 2 ns^d
+// whose points share one cell is summed in registers -- in 3D (ns >= 5)
+// lane (x, y0) owns the taps (x, y0 + m 32/ns, z) for every z, otherwise
+// lane l takes the taps l, l + 32, ..., four at a time -- from the points'
+// kernel values staged in warp-private shared memory, then each tap sum is
+// added to the tile once (conflict-free: the lanes' taps differ).  Any other
+// chunk is spread point by point with shared atomics, lanes over x taps as
+// in k_spread_sm_wc.  Dense chunks thus cost FMAs instead of 2 ns^d
 // same-address atomics per point.  Taps per point <= 512.  Subproblems that
-// start on a sparse cell are left to k_spread_sm_wc (its higher occupancy
-// wins there), launched beside this kernel.
+// start on a sparse cell, and (split) the sparse tails of the others, are
+// left to the sparse kernel launched beside this one (slab-owned in 3D,
+// private-tile in 2D, warp-cooperative otherwise).
 template <int DIM, int NS> constexpr int run_taps() {
   return DIM == 1 ? NS : (DIM == 2 ? NS * NS : NS * NS * NS);
 }
@@ -1774,9 +1776,14 @@ inline bool tc_spread_enabled() {
 }
 
 // Kernel family per stage (SpreadArgs::variant 0 = the measured default):
-// spreading is warp-cooperative for both methods; interpolation is
-// warp-cooperative for method 1 and one-thread-per-point for method 2.
-// variant 1 forces one thread per point, 2 forces warp-cooperative.
+// spreading is warp-cooperative for method 1; for method 2 it is the
+// slab-owned kernel in 3D and the private-tile kernel in 2D (the
+// warp-cooperative atomic kernel in 1D, and wherever their shared memory does
+// not fit), with the cell-run kernel on dense prefixes of the cell-run
+// layout; interpolation is warp-cooperative for method 1 and
+// one-thread-per-point for method 2 (double-float for FP64 plans at
+// tol >= 1e-13).  variant 1 forces one thread per point, 2 forces
+// warp-cooperative.
 template <typename T, int DIM, int NS>
 cudaError_t spread_ns(int method, const SpreadArgs<T>& a, cudaStream_t s) {
   if (a.M == 0) return cudaSuccess;
