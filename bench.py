@@ -19,7 +19,9 @@ ns = ceil(-log10(tol/10)) leaves errors of one to four times tol, so its
 throughput is reported beside the headline as `parity_width`, and --width-rule
 reference times it instead.  The default run also times, device time only,
 the 3D clustered type-1 workload and the uneven 64-plan batch (tuned+batched
-against 64 plain plans) under `extra_workloads` (--no-extras skips them).  `value` times execute() on device-resident inputs with CUDA events
+against 64 plain plans, and against the same plain plans spreading with the
+reference's per-tap shared atomics) under `extra_workloads` (--no-extras
+skips them).  `value` times execute() on device-resident inputs with CUDA events
 on the plan's stream (L2 flushed with a 256 MB write between steps, outside
 the timed events); `e2e` times the same public call with the input copied
 from pinned host memory and the output copied back inside each step.
@@ -902,6 +904,22 @@ def run_batch64(args, rank, world, local_rank, extra=False):
         run_plain()
     plain_graph_ms = timed(run_plain, args.steps)
     out_plain = [f.cpu().numpy() for f in fks[:8]]
+    # and with the reference's subproblem algorithm for method 2 -- per-tap
+    # shared-memory atomicAdd into one tile per subproblem -- in place of the
+    # library's private-tile kernel (CUFINUFFT_SPREAD_PRIV=0), launched directly
+    saved_env = {k: os.environ.get(k) for k in ("CUFINUFFT_GRAPH", "CUFINUFFT_SPREAD_PRIV")}
+    os.environ["CUFINUFFT_GRAPH"] = "0"
+    os.environ["CUFINUFFT_SPREAD_PRIV"] = "0"
+    try:
+        for _ in range(args.warmup):
+            run_plain()
+        plain_atomic_ms = timed(run_plain, args.steps)
+    finally:
+        for k, v in saved_env.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     del plain
 
     # batched with the library's default choice (gpu_method 0), one graph
@@ -1000,8 +1018,15 @@ def run_batch64(args, rank, world, local_rank, extra=False):
                           "after another on one stream, kernels launched directly as the "
                           "reference launches them (CUFINUFFT_GRAPH=0)",
                   "graph_replay_ms_per_step": plain_graph_ms},
+        "plain_shared_atomic": {
+            "ms_per_step": plain_atomic_ms,
+            "note": "the same 64 plain plans, launched directly, with method-2 spreading by "
+                    "per-tap shared-memory atomicAdd into one tile per subproblem (the "
+                    "reference's subproblem algorithm, src/2d/spreadinterp2d.cu "
+                    "Spread_2d_Subprob) instead of the library's private-tile kernel"},
         "speedup_vs_plain": plain_ms / batch_ms,
         "speedup_vs_plain_graph_replay": plain_graph_ms / batch_ms,
+        "speedup_vs_plain_shared_atomic": plain_atomic_ms / batch_ms,
         "batched_default_ms": default_ms, "batched_tuned_warmup_ms": tuned_warm_ms,
         "autotune": {"seconds": tune_s, "policy": policy,
                      "per_plan_choice": {f"method {m} bins {b}" + (f" maxsub {c}" if c else ""): n
