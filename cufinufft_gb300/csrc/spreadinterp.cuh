@@ -967,11 +967,26 @@ __host__ __device__ constexpr int slab_pitch(int tx, int ns) {
   return tx + (((ns - tx) % 16) + 16) % 16;
 }
 
+// FP32 kernel rows along y staged in pairs, for widths whose point takes two
+// or more row instructions (R = 32 / ns rows each, NR of them): slot
+// m R + y holds (ky[2m R + y], ky[(2m + 1) R + y]), so lane (dx, y) reads one
+// float2 per two row instructions instead of one float per instruction.
+// Point q of a stage of n points sits at slot (n + 1) + q: the R slots one
+// instruction reads are 8 (n + 1) bytes apart, two banks apart for n = 32 or
+// 64 (distinct banks, one wavefront), and consecutive points are consecutive
+// words (conflict-free staging stores).
+__host__ __device__ constexpr int ky_rows_per_instr(int ns) { return 32 / ns; }
+__host__ __device__ constexpr int ky_instrs(int ns) { return (ns + 32 / ns - 1) / (32 / ns); }
+__host__ __device__ constexpr bool ky_paired(int ns, int real_bytes) { return real_bytes == 4 && ky_instrs(ns) >= 2; }
+__host__ __device__ constexpr int ky_pair_slots(int ns) { return (ky_instrs(ns) + 1) / 2 * ky_rows_per_instr(ns); }
+
 template <typename T>
 size_t slab_bytes(int ns, const BinTables& bt) {
   const size_t px = slab_pitch(bt.bs[0] + ns - 1, ns);
   const size_t cells = px * (bt.bs[1] + ns - 1) * (bt.bs[2] + ns - 1);
-  const size_t stage = (size_t)kSlabChunk * ns * (sizeof(cplx_t<T>) + 2 * sizeof(T)) + kSlabChunk * sizeof(int2);
+  const size_t ky = ky_paired(ns, sizeof(T)) ? (size_t)ky_pair_slots(ns) * (kSlabChunk + 1) * sizeof(float2)
+                                             : (size_t)kSlabChunk * ns * sizeof(T);
+  const size_t stage = (size_t)kSlabChunk * ns * (sizeof(cplx_t<T>) + sizeof(T)) + ky + kSlabChunk * sizeof(int2);
   return cells * sizeof(cplx_t<T>) + 16 + 2 * stage;  // stage aligned to 16 bytes
 }
 
@@ -1004,6 +1019,8 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
   constexpr int R = 32 / NS;                 // tile rows per warp instruction
   constexpr int NR = (NS + R - 1) / R;       // instructions per plane
   constexpr int CH = kSlabChunk;
+  constexpr bool kPairs = ky_paired(NS, sizeof(T));
+  constexpr int NPR = (NR + 1) / 2;          // ky pairs per lane (kPairs)
   // cell-run layout: a subproblem that starts on a dense cell leaves its
   // leading dense points to k_spread_sm_run (split) or all of them (not)
   int first = 0;
@@ -1018,10 +1035,13 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
   const int PP = PX * st.TY;                  // plane stride
   const int ncell = PP * st.TZ;
   C* tile = reinterpret_cast<C*>(smem_raw);
-  // double-buffered stage: [c kx (complex) | ky | kz] x CH x NS, then
-  // (tile offset, lz mod NS) per point
+  // double-buffered stage: [c kx (complex) | kz] x CH x NS, ky (CH x NS, or
+  // in pairs: ky_pair_slots x (CH + 1) float2), then (tile offset, lz mod NS)
+  // per point
   unsigned char* stage0 = smem_raw + (((size_t)ncell * sizeof(C) + 15) & ~(size_t)15);
-  const size_t stage_sz = (size_t)CH * NS * (sizeof(C) + 2 * sizeof(T)) + CH * sizeof(int2);
+  constexpr size_t kKyBytes =
+      kPairs ? (size_t)ky_pair_slots(NS) * (CH + 1) * sizeof(float2) : (size_t)CH * NS * sizeof(T);
+  const size_t stage_sz = (size_t)CH * NS * (sizeof(C) + sizeof(T)) + kKyBytes + CH * sizeof(int2);
   const int t = blockIdx.y;
   for (int i = threadIdx.x; i < ncell; i += blockDim.x) tile[i] = C{T(0), T(0)};
   const C* cin = a.c_in + (size_t)t * a.M;
@@ -1032,9 +1052,9 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
   for (int c0 = first, buf = 0; c0 < st.np; c0 += CH, buf ^= 1) {
     unsigned char* sb = stage0 + buf * stage_sz;
     C* s_ck = reinterpret_cast<C*>(sb);
-    T* s_ky = reinterpret_cast<T*>(s_ck + CH * NS);
-    T* s_kz = s_ky + CH * NS;
-    int2* s_bl = reinterpret_cast<int2*>(s_kz + CH * NS);
+    T* s_kz = reinterpret_cast<T*>(s_ck + CH * NS);
+    T* s_ky = s_kz + CH * NS;  // kPairs: float2 slots, see ky_pair_slots
+    int2* s_bl = reinterpret_cast<int2*>(reinterpret_cast<unsigned char*>(s_ky) + kKyBytes);
     const int nq = min(CH, st.np - c0);
     for (int i = threadIdx.x; i < nq * NS; i += blockDim.x) {
       const int q = i / NS, j = i - q * NS;
@@ -1042,7 +1062,13 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
       const C v = cin[a.pts.idx[p]];
       const T kx = kernel_tap<T, NS, HD>(a.pts.d[0][p], j, a.kc);
       s_ck[i] = C{v.x * kx, v.y * kx};
-      s_ky[i] = kernel_tap<T, NS, HD>(a.pts.d[1][p], j, a.kc);
+      const T kyj = kernel_tap<T, NS, HD>(a.pts.d[1][p], j, a.kc);
+      if constexpr (kPairs) {
+        const int r = j / R, y = j - r * R;  // row instruction and lane row of tap j
+        s_ky[(((r >> 1) * R + y) * (CH + 1) + q) * 2 + (r & 1)] = kyj;
+      } else {
+        s_ky[i] = kyj;
+      }
       s_kz[i] = kernel_tap<T, NS, HD>(a.pts.d[2][p], j, a.kc);
       if (j == 0) {
         const int lx = a.pts.i0[0][p] - st.ox, ly = a.pts.i0[1][p] - st.oy, lz = a.pts.i0[2][p] - st.oz;
@@ -1058,14 +1084,26 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
       const C ck = s_ck[q * NS + dx];
       const T ur = ck.x * kz, ui = ck.y * kz;
       const int base = bl.x + dz * PP + dx;
+      T ky[NR];
+      if constexpr (kPairs) {
+        const float2* kp = reinterpret_cast<const float2*>(s_ky) + min(dyl, R - 1) * (CH + 1) + q;
+#pragma unroll
+        for (int m = 0; m < NPR; ++m) {
+          const float2 v = kp[m * R * (CH + 1)];
+          ky[2 * m] = v.x;
+          if (2 * m + 1 < NR) ky[2 * m + 1] = v.y;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < NR; ++r) ky[r] = s_ky[q * NS + min(r * R + dyl, NS - 1)];
+      }
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
         const int dy = r * R + dyl;
         if (kFullRows || (lane_on && dy < NS)) {
-          const T ky = s_ky[q * NS + dy];
           C v = tile[base + dy * PX];
-          v.x = fma_rn(ur, ky, v.x);
-          v.y = fma_rn(ui, ky, v.y);
+          v.x = fma_rn(ur, ky[r], v.x);
+          v.y = fma_rn(ui, ky[r], v.y);
           tile[base + dy * PX] = v;
         }
       }
@@ -1091,12 +1129,20 @@ k_spread_sm_slab(SpreadArgs<T> a, int split) {
 // to the order of additions.
 constexpr int kPrivWarps = 4;
 
+// Bytes of one warp's stage: c kx (complex), ky (32 x ns, or in pairs:
+// ky_pair_slots x 33 float2), the tile offset.
+__host__ __device__ constexpr size_t priv_stage_bytes(int ns, int real_bytes) {
+  return (32 * (size_t)ns * 2 * real_bytes +
+          (ky_paired(ns, real_bytes) ? (size_t)ky_pair_slots(ns) * 33 * 8 : 32 * (size_t)ns * real_bytes) +
+          32 * sizeof(int) + 15) &
+         ~(size_t)15;
+}
+
 template <typename T>
 size_t priv_bytes(int ns, const BinTables& bt) {
   const size_t px = slab_pitch(bt.bs[0] + ns - 1, ns);
   const size_t copy = px * (bt.bs[1] + ns - 1) * sizeof(cplx_t<T>);
-  const size_t stage = 32 * (size_t)ns * (sizeof(cplx_t<T>) + sizeof(T)) + 32 * sizeof(int);
-  return kPrivWarps * (((copy + 15) & ~(size_t)15) + ((stage + 15) & ~(size_t)15));
+  return kPrivWarps * (((copy + 15) & ~(size_t)15) + priv_stage_bytes(ns, sizeof(T)));
 }
 
 template <typename T, int NS>
@@ -1106,6 +1152,8 @@ k_spread_sm_priv(SpreadArgs<T> a, int split) {
   constexpr int R = 32 / NS;                 // tile rows per warp instruction
   constexpr int NR = (NS + R - 1) / R;       // instructions per point
   constexpr int HD = horner_degree<T>(NS);
+  constexpr bool kPairs = ky_paired(NS, sizeof(T));
+  constexpr int NPR = (NR + 1) / 2;          // ky pairs per lane (kPairs)
   int first = 0;
   if (a.sub_dense && a.sub_dense[blockIdx.x]) {  // cell-run layout: dense prefixes by k_spread_sm_run
     if (!split) return;
@@ -1117,13 +1165,14 @@ k_spread_sm_priv(SpreadArgs<T> a, int split) {
   const int PX = slab_pitch(st.TX, NS);
   const int ncell = PX * st.TY;
   const size_t copy_sz = ((size_t)ncell * sizeof(C) + 15) & ~(size_t)15;
-  const size_t stage_sz = ((size_t)32 * NS * (sizeof(C) + sizeof(T)) + 32 * sizeof(int) + 15) & ~(size_t)15;
+  constexpr size_t stage_sz = priv_stage_bytes(NS, sizeof(T));
+  constexpr size_t kKyBytes = kPairs ? (size_t)ky_pair_slots(NS) * 33 * sizeof(float2) : (size_t)32 * NS * sizeof(T);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   C* tile = reinterpret_cast<C*>(smem_raw + warp * copy_sz);
   unsigned char* sb = smem_raw + kPrivWarps * copy_sz + warp * stage_sz;
   C* s_ck = reinterpret_cast<C*>(sb);
-  T* s_ky = reinterpret_cast<T*>(s_ck + 32 * NS);
-  int* s_base = reinterpret_cast<int*>(s_ky + 32 * NS);
+  T* s_ky = reinterpret_cast<T*>(s_ck + 32 * NS);  // kPairs: float2 slots, see ky_pair_slots
+  int* s_base = reinterpret_cast<int*>(reinterpret_cast<unsigned char*>(s_ky) + kKyBytes);
   for (int i = lane; i < ncell; i += 32) tile[i] = C{T(0), T(0)};
   const int t = blockIdx.y;
   const C* cin = a.c_in + (size_t)t * a.M;
@@ -1159,26 +1208,51 @@ k_spread_sm_priv(SpreadArgs<T> a, int split) {
 #pragma unroll
       for (int j = 0; j < NS; ++j) s_ck[lane * NS + j] = C{cv.x * kr[j], cv.y * kr[j]};
       kernel_row<T, NS, HD>(d1, a.kc, kr);
+      if constexpr (kPairs) {
+        float2* kp = reinterpret_cast<float2*>(s_ky) + lane;
 #pragma unroll
-      for (int j = 0; j < NS; ++j) s_ky[lane * NS + j] = kr[j];
+        for (int m = 0; m < NPR; ++m)
+#pragma unroll
+          for (int y = 0; y < R; ++y) {
+            const int j0 = 2 * m * R + y, j1 = j0 + R;
+            kp[(m * R + y) * 33] = make_float2(j0 < NS ? kr[j0] : 0.f, j1 < NS ? kr[j1] : 0.f);
+          }
+      } else {
+#pragma unroll
+        for (int j = 0; j < NS; ++j) s_ky[lane * NS + j] = kr[j];
+      }
       s_base[lane] = (i01 - st.oy) * PX + (i00 - st.ox);
     }
     if (c0 + 32 < end) load_pt(c0 + 32);
     __syncwarp();
     // the next point's staged values are read while this point's cells are
     // read, added to and written
+    // lane (dx, dyl)'s y rows of point q: one float2 per pair of row
+    // instructions (kPairs), else one value per instruction
+    auto load_ky = [&](int q, T* ky) {
+      if constexpr (kPairs) {
+        const float2* kp = reinterpret_cast<const float2*>(s_ky) + min(dyl, R - 1) * 33 + q;
+#pragma unroll
+        for (int m = 0; m < NPR; ++m) {
+          const float2 v = kp[m * R * 33];
+          ky[2 * m] = v.x;
+          if (2 * m + 1 < NR) ky[2 * m + 1] = v.y;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < NR; ++r) ky[r] = s_ky[q * NS + min(r * R + dyl, NS - 1)];
+      }
+    };
     C ck = s_ck[dx];
     int base = s_base[0] + dx;
     T ky[NR];
-#pragma unroll
-    for (int r = 0; r < NR; ++r) ky[r] = s_ky[min(r * R + dyl, NS - 1)];
+    load_ky(0, ky);
     for (int q = 0; q < nq; ++q) {
       const int qn = min(q + 1, nq - 1);
       const C ckn = s_ck[qn * NS + dx];
       const int basen = s_base[qn] + dx;
       T kyn[NR];
-#pragma unroll
-      for (int r = 0; r < NR; ++r) kyn[r] = s_ky[qn * NS + min(r * R + dyl, NS - 1)];
+      load_ky(qn, kyn);
 #pragma unroll
       for (int r = 0; r < NR; ++r) {
         const int dy = r * R + dyl;
