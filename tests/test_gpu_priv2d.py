@@ -26,6 +26,7 @@ CASES = [
     ((64, 60), 30000, True, 1e-2, (16, 16), 3),
     ((90, 70), 40000, True, 1e-4, (64, 64), 2),
     ((50, 70), 20000, True, 1e-5, (24, 40), 1),
+    ((48, 40), 10000, True, 1e-8, (16, 16), 2),     # FP32 ns 9 (its cap at sigma 2): two pairs of y rows
     ((48, 40), 10000, False, 1e-12, (32, 32), 2),
     ((48, 40), 10000, False, 1e-9, (16, 16), 1),
     ((40, 40), 8000, False, 1e-15, (8, 8), 1),

@@ -24,6 +24,7 @@ CASES = [
     ((24, 20, 18), 20000, True, 1e-6, 2, (8, 8, 8), 2, "tol"),   # ns 8: full-lane rows
     ((24, 20, 18), 20000, True, 1e-2, 2, (8, 8, 8), 3),
     ((30, 28, 26), 30000, True, 1e-4, 2, (16, 16, 4), 2),
+    ((16, 18, 20), 8000, True, 1e-8, 2, (8, 8, 8), 2),      # FP32 ns 9 (its cap at sigma 2): two pairs of y rows
     ((16, 18, 20), 8000, False, 1e-12, 2, (8, 8, 8), 2),
     ((16, 18, 20), 8000, False, 1e-9, 2, (16, 16, 2), 1),
     ((16, 18, 20), 8000, False, 1e-15, 2, (4, 4, 4), 1),

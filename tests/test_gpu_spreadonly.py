@@ -87,3 +87,40 @@ def test_autotuned_spread_only_plan(ntype):
     ref = _oracle(ntype, grid, pts, data, 1e-6, True, 1)
     err = np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
     assert err < 1e-5, err
+
+
+@pytest.mark.parametrize("grid,bins,tol", [((64, 60), (16, 16), 1e-5), ((64, 60), (32, 32), 1e-6),
+                                           ((32, 30, 28), (8, 8, 8), 1e-6)])
+def test_wide_fp32_kernels_on_the_subproblem_spreads(monkeypatch, grid, bins, tol):
+    """FP32 reaches widths above 9 only at upsampling factor 1.25 (9..12
+    here), where the private-tile (2D) and slab (3D) spreads stage two or
+    three pairs of y kernel rows per lane.  On the grid itself (spread-only:
+    no deconvolution, which at sigma 1.25 amplifies FP32 rounding) the
+    default kernel must match the shared-atomic kernel to FP32 rounding and
+    the oracle's spread at the same width."""
+    rng = np.random.default_rng(len(grid) * 100 + bins[0])
+    M, ntr = 6000, 2
+    pts = NC.points(rng, len(grid), M, edges=False)
+    c = NC.strengths(rng, M, ntr)
+    kw = dict(ntr=ntr, gpu_method=2, gpu_spreadinterponly=1, maxbatchsize=2, upsampfac=1.25,
+              width_rule="tol", gpu_binsizex=bins[0], gpu_binsizey=bins[1])
+    if len(grid) == 3:
+        kw["gpu_binsizez"] = bins[2]
+    env = "CUFINUFFT_SPREAD_PRIV" if len(grid) == 2 else "CUFINUFFT_SPREAD_SLAB"
+    monkeypatch.setenv(env, "0")
+    ref_atomic, _ = NC.run_gpu(1, grid, pts, c, tol, True, **kw)
+    monkeypatch.delenv(env)
+    out, info = NC.run_gpu(1, grid, pts, c, tol, True, **kw)
+    assert info["ns"] >= 9, info["ns"]
+    # norms in FP64: the ES kernel is unnormalised (peak e^beta, ~3e9 per axis
+    # at ns 12), so 3D grid values reach ~1e29 and their squares overflow FP32
+    out = out.astype(np.complex128)
+    ref_atomic = ref_atomic.astype(np.complex128)
+    err = np.linalg.norm(out.ravel() - ref_atomic.ravel()) / np.linalg.norm(ref_atomic.ravel())
+    assert err < 1e-6, (info["ns"], err)
+    plan = O.OraclePlan(1, grid, 1, tol, True, spreadinterponly=True, upsampfac=1.25, ns=info["ns"])
+    args = list(pts) + [None] * (3 - len(pts))
+    ref = plan.spread(*args, c=c, ntr=ntr)
+    err = np.linalg.norm(out.ravel() - ref.ravel()) / np.linalg.norm(ref.ravel())
+    assert err < 1e-5, (info["ns"], err)
+
